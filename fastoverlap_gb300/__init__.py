@@ -1,0 +1,18 @@
+"""fastoverlap_gb300 -- GB300 (sm_103a) implementation of the FASTOVERLAP
+alignment path.
+
+Public classes keep the upstream names and signatures:
+    SphericalAlign, SphericalAlignFortran   (cluster alignment)
+    PeriodicAlign, PeriodicAlignFortran     (periodic alignment)
+Batched and resident forms:
+    align_clusters, align_periodic, ClusterBatch, BulkBatch
+All compute runs in libfastoverlap_gb300.so (CUDA); there is no CPU path.
+"""
+from ._lib import Context, FoError, default_context, load  # noqa: F401
+from .batch import BulkBatch, ClusterBatch, align_clusters, align_periodic  # noqa: F401
+from .periodicAlignment import PeriodicAlign, PeriodicAlignFortran  # noqa: F401
+from .sphericalAlignment import SphericalAlign, SphericalAlignFortran  # noqa: F401
+
+__all__ = ["SphericalAlign", "SphericalAlignFortran", "PeriodicAlign", "PeriodicAlignFortran",
+           "align_clusters", "align_periodic", "ClusterBatch", "BulkBatch", "Context",
+           "FoError", "default_context", "load"]

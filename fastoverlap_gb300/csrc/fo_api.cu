@@ -1,0 +1,821 @@
+// fo_api.cu -- the C ABI (include/fastoverlap_gb300.h): context, Wigner-table
+// cache, batch plans (validation, device layout, upload), pipeline launch
+// and result download, plus the Fortran-style single-pair entry points.
+#include "../../include/fastoverlap_gb300.h"
+#include "fo_common.cuh"
+#include "fo_kernels.h"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace fo {
+size_t refine_smem_bytes(int maxn);
+long long lap_bytes_host(int maxg);
+}  // namespace fo
+
+namespace {
+
+constexpr int kMaxAtoms = 2000;  // refinement keeps 4 coordinate copies in shared memory
+constexpr int kMaxJmax = 31;     // SO(3) grid <= 64^3 (two 64x64 complex slices on chip)
+constexpr int kMaxNrot = 64;
+constexpr int kMaxM = 256;
+
+int fastlen(int n) {
+    if (n <= 1) return 1;
+    for (int m = n;; ++m) {
+        int k = m;
+        while (k % 2 == 0) k /= 2;
+        while (k % 3 == 0) k /= 3;
+        while (k % 5 == 0) k /= 5;
+        if (k == 1) return m;
+    }
+}
+
+const int kNumKernels = 16;
+const char *kKernelNames[kNumKernels] = {
+    "sph_center", "sph_ylm",    "sph_radial", "sph_coeff", "isoft",      "findpeaks",
+    "refine",     "select",     "bulk_prep",  "bulk_sf",   "bulk_fft",   "memset",
+    "wigner",     "h2d",        "d2h",        "other"};
+enum KId { K_CENTER, K_YLM, K_RADIAL, K_COEFF, K_ISOFT, K_PEAKS, K_REFINE, K_SELECT, K_BPREP,
+           K_BSF, K_BFFT, K_MEMSET, K_WIGNER, K_H2D, K_D2H, K_OTHER };
+
+}  // namespace
+
+struct fo_ctx {
+    fo_opts opts;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::map<int, std::pair<double *, float *>> dtab;
+    double **d_dtab64 = nullptr;
+    float **d_dtab32 = nullptr;
+    std::vector<int> permgroup, npermsize;
+    int perm_natoms = 0;
+    std::vector<int> bestperm;
+    double prof_ms[kNumKernels] = {0};
+    int prof_n[kNumKernels] = {0};
+};
+
+struct fo_plan {
+    fo_ctx *ctx = nullptr;
+    bool bulk = false, fp32 = false;
+    int npairs = 0, nslots = 0, ncand = 0, ngroups = 0;
+    int maxL = 0, maxG = 0, maxgroup = 0, maxn = 0;
+    int index_base = 0;
+    std::vector<fo::PairDev> hp;
+    std::vector<fo::GroupDev> hg;
+    std::vector<long long> caller_off;  // caller's atom offset per pair
+    unsigned char *dmem = nullptr;
+    size_t dbytes = 0;
+    fo::SphBuffers sb{};
+    fo::BulkBuffers bb{};
+    fo::RefineBuffers rb{};
+    size_t coef_bytes = 0, fgrid_bytes = 0;
+    int *d_pstatus = nullptr, *d_npeaks = nullptr;
+    void *d_coef = nullptr, *d_fgrid = nullptr;
+    std::vector<cudaEvent_t> evs;
+    std::vector<int> ev_kid;
+};
+
+namespace {
+
+fo_status set_err(fo_ctx *ctx, fo_status s, const char *fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return s;
+}
+
+fo_status cuda_check(fo_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return FO_OK;
+    return set_err(ctx, FO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// ensure Wigner tables exist for every bandwidth in [1, maxbw] that is used
+fo_status ensure_dtabs(fo_ctx *ctx, const std::vector<int> &bws) {
+    int maxbw = 0;
+    for (int b : bws) maxbw = std::max(maxbw, b);
+    for (int bw : bws) {
+        if (ctx->dtab.count(bw)) continue;
+        int W = 2 * bw - 1;
+        size_t n = (size_t)2 * bw * W * W * bw;
+        double *d64 = nullptr;
+        float *d32 = nullptr;
+        fo_status s = cuda_check(ctx, cudaMalloc(&d64, n * sizeof(double)), "cudaMalloc(wigner)");
+        if (s) return s;
+        s = cuda_check(ctx, cudaMalloc(&d32, n * sizeof(float)), "cudaMalloc(wigner32)");
+        if (s) { cudaFree(d64); return s; }
+        fo::launch_wigner_table(bw, d64, d32, ctx->stream);
+        ctx->dtab[bw] = {d64, d32};
+    }
+    // rebuild the device pointer tables indexed by bandwidth
+    int cap = 65;
+    std::vector<double *> h64(cap, nullptr);
+    std::vector<float *> h32(cap, nullptr);
+    for (auto &kv : ctx->dtab)
+        if (kv.first < cap) { h64[kv.first] = kv.second.first; h32[kv.first] = kv.second.second; }
+    if (!ctx->d_dtab64) {
+        fo_status s = cuda_check(ctx, cudaMalloc(&ctx->d_dtab64, cap * sizeof(double *)), "cudaMalloc");
+        if (s) return s;
+        s = cuda_check(ctx, cudaMalloc(&ctx->d_dtab32, cap * sizeof(float *)), "cudaMalloc");
+        if (s) return s;
+    }
+    fo_status s = cuda_check(ctx, cudaMemcpyAsync(ctx->d_dtab64, h64.data(), cap * sizeof(double *),
+                                                  cudaMemcpyHostToDevice, ctx->stream), "copy");
+    if (s) return s;
+    s = cuda_check(ctx, cudaMemcpyAsync(ctx->d_dtab32, h32.data(), cap * sizeof(float *),
+                                        cudaMemcpyHostToDevice, ctx->stream), "copy");
+    if (s) return s;
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "wigner tables");
+}
+
+// validate the permutation groups of one pair and fill slot2orig
+fo_status check_groups(fo_ctx *ctx, int i, int n, int ngroups, const int *perm,
+                       const int *gsizes, int base, int *slot2orig) {
+    if (ngroups < 1) return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: ngroups < 1", i);
+    long long tot = 0;
+    for (int g = 0; g < ngroups; ++g) {
+        if (gsizes[g] < 0) return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: negative group size", i);
+        tot += gsizes[g];
+    }
+    if (tot != n)
+        return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: groups hold %lld atoms, natoms = %d", i, tot, n);
+    std::vector<char> seen(n, 0);
+    for (int s = 0; s < n; ++s) {
+        int a = perm[s] - base;
+        if (a < 0 || a >= n) return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: atom index %d out of range", i, perm[s]);
+        if (seen[a]) return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: atom %d in two groups", i, perm[s]);
+        seen[a] = 1;
+        slot2orig[s] = a;
+    }
+    return FO_OK;
+}
+
+struct Carve {
+    size_t off = 0;
+    template <typename T> size_t take(size_t count) {
+        size_t o = off;
+        off += align256(count * sizeof(T));
+        return o;
+    }
+};
+
+void rec_event(fo_plan *pl, int kid) {
+    if (!pl->ctx->opts.profile) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, pl->ctx->stream);
+    pl->evs.push_back(e);
+    pl->ev_kid.push_back(kid);
+}
+
+fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
+    size_t budget = ctx->opts.hbm_budget_bytes;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = (size_t)(0.8 * fr);
+    }
+    if (bytes > budget)
+        return set_err(ctx, FO_ERR_OOM_BUDGET, "plan needs %zu bytes, budget %zu", bytes, budget);
+    fo_status s = cuda_check(ctx, cudaMalloc(&pl->dmem, bytes), "cudaMalloc(plan)");
+    if (s) return s;
+    pl->dbytes = bytes;
+    return FO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fo_status_string(fo_status s) {
+    switch (s) {
+        case FO_OK: return "ok";
+        case FO_ERR_BAD_ARGS: return "bad arguments";
+        case FO_ERR_NO_PEAKS: return "no peaks found";
+        case FO_ERR_LAP_FAILED: return "assignment failed";
+        case FO_ERR_TIMEOUT: return "timeout";
+        case FO_ERR_OOM_BUDGET: return "HBM budget exceeded";
+        case FO_ERR_CUDA: return "CUDA error";
+        case FO_ERR_UNIMPLEMENTED: return "unimplemented";
+        case FO_ERR_QUEUE_FULL: return "queue full";
+        case FO_ERR_NOT_READY: return "not ready";
+    }
+    return "unknown";
+}
+
+const char *fo_last_error(const fo_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+fo_status fo_ctx_create(const fo_opts *opts, fo_ctx **out) {
+    if (!out) return FO_ERR_BAD_ARGS;
+    *out = nullptr;
+    fo_ctx *c = new fo_ctx();
+    if (opts) c->opts = *opts;
+    else {
+        memset(&c->opts, 0, sizeof c->opts);
+        c->opts.cutoff = 1;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        delete c;
+        return FO_ERR_CUDA;
+    }
+    if (c->opts.device < 0 || c->opts.device >= ndev) { delete c; return FO_ERR_BAD_ARGS; }
+    if (cudaSetDevice(c->opts.device) != cudaSuccess) { delete c; return FO_ERR_CUDA; }
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return FO_ERR_CUDA;
+    }
+    *out = c;
+    return FO_OK;
+}
+
+void fo_ctx_destroy(fo_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->opts.device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->dtab) { cudaFree(kv.second.first); cudaFree(kv.second.second); }
+    cudaFree(ctx->d_dtab64);
+    cudaFree(ctx->d_dtab32);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+fo_status fo_set_precision(fo_ctx *ctx, int precision) {
+    if (!ctx || (precision != FO_PREC_FP64 && precision != FO_PREC_MIXED)) return FO_ERR_BAD_ARGS;
+    ctx->opts.precision = precision;
+    return FO_OK;
+}
+
+// ---------------------------------------------------------------------------
+static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1, const double *pos2,
+                                   const std::vector<int> &slot2orig, const std::vector<int> &slot2pair,
+                                   const std::vector<int> &cand2pair, size_t ylm_n, size_t w_n,
+                                   size_t coef_n, size_t grid_n, size_t fgrid_n, long long lap_total) {
+    const size_t T = pl->fp32 ? 4 : 8;
+    const int np = pl->npairs, ns = pl->nslots, nc = pl->ncand;
+    Carve cv;
+    size_t o_pairs = cv.take<fo::PairDev>(np), o_groups = cv.take<fo::GroupDev>(pl->ngroups);
+    size_t o_s2o = cv.take<int>(ns), o_s2p = cv.take<int>(ns), o_c2p = cv.take<int>(nc);
+    size_t o_pos1 = cv.take<double>(3 * (size_t)ns), o_pos2 = cv.take<double>(3 * (size_t)ns);
+    size_t o_xa = cv.take<double>(3 * (size_t)ns), o_xb = cv.take<double>(3 * (size_t)ns);
+    size_t o_ra = cv.take<double>(ns), o_rb = cv.take<double>(ns);
+    size_t o_ylmA = cv.take<char>(ylm_n * 2 * T), o_ylmB = cv.take<char>(ylm_n * 2 * T);
+    size_t o_W = cv.take<char>(w_n * T);
+    size_t o_coef = cv.take<char>(coef_n * 2 * T);
+    size_t o_grid = cv.take<char>(grid_n * T);
+    size_t o_fgrid = cv.take<char>(fgrid_n * 2 * T);
+    size_t o_omax = cv.take<double>(2 * (size_t)np), o_peaks = cv.take<double>(3 * (size_t)nc);
+    size_t o_npk = cv.take<int>(2 * (size_t)np), o_pst = cv.take<int>(np);
+    size_t o_lap = cv.take<unsigned char>((size_t)lap_total);
+    size_t candatoms = 0;
+    for (auto &P : pl->hp) candatoms += (size_t)P.norient * P.nrot * P.n;
+    size_t o_cdist = cv.take<double>(nc), o_cR = cv.take<double>(9 * (size_t)nc),
+           o_cdisp = cv.take<double>(3 * (size_t)nc);
+    size_t o_cxyz = cv.take<double>(3 * candatoms), o_cperm = cv.take<int>(candatoms);
+    size_t o_cnit = cv.take<int>(nc), o_cst = cv.take<int>(nc);
+    size_t o_res = cv.take<fo_pair_result>(np), o_al = cv.take<double>(3 * (size_t)ns),
+           o_pb = cv.take<int>(ns);
+    fo_status s = finish_plan_alloc(ctx, pl, cv.off);
+    if (s) return s;
+    unsigned char *m = pl->dmem;
+    auto P = [&](size_t o) { return (void *)(m + o); };
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(P(o_pairs), pl->hp.data(), np * sizeof(fo::PairDev), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(P(o_groups), pl->hg.data(), pl->ngroups * sizeof(fo::GroupDev), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(P(o_s2o), slot2orig.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(P(o_s2p), slot2pair.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(P(o_c2p), cand2pair.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(P(o_pos1), pos1, 3 * (size_t)ns * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(P(o_pos2), pos2, 3 * (size_t)ns * sizeof(double), cudaMemcpyHostToDevice, st);
+    s = cuda_check(ctx, cudaStreamSynchronize(st), "plan upload");
+    if (s) return s;
+
+    pl->sb.pairs = (const fo::PairDev *)P(o_pairs);
+    pl->sb.groups = (const fo::GroupDev *)P(o_groups);
+    pl->sb.slot2orig = (const int *)P(o_s2o);
+    pl->sb.slot2pair = (const int *)P(o_s2p);
+    pl->sb.pos1 = (const double *)P(o_pos1);
+    pl->sb.pos2 = (const double *)P(o_pos2);
+    pl->sb.xa = (double *)P(o_xa);
+    pl->sb.xb = (double *)P(o_xb);
+    pl->sb.ra = (double *)P(o_ra);
+    pl->sb.rb = (double *)P(o_rb);
+    pl->sb.ylmA = P(o_ylmA);
+    pl->sb.ylmB = P(o_ylmB);
+    pl->sb.W = P(o_W);
+    pl->sb.coef = P(o_coef);
+    pl->sb.grid = P(o_grid);
+    pl->sb.npairs = np;
+    pl->sb.ngroups = pl->ngroups;
+    pl->sb.nslots = ns;
+    pl->sb.maxL = pl->maxL;
+    pl->sb.maxG = pl->maxG;
+    pl->sb.maxgroup = pl->maxgroup;
+    pl->d_coef = P(o_coef);
+    pl->coef_bytes = coef_n * 2 * T;
+    pl->d_fgrid = P(o_fgrid);
+    pl->fgrid_bytes = fgrid_n * 2 * T;
+
+    pl->bb.pairs = pl->sb.pairs;
+    pl->bb.groups = pl->sb.groups;
+    pl->bb.slot2orig = pl->sb.slot2orig;
+    pl->bb.pos1 = pl->sb.pos1;
+    pl->bb.pos2 = pl->sb.pos2;
+    pl->bb.xa = pl->sb.xa;
+    pl->bb.xb = pl->sb.xb;
+    pl->bb.fgrid = P(o_fgrid);
+    pl->bb.grid = P(o_grid);
+    pl->bb.npairs = np;
+    pl->bb.maxK = pl->maxL;
+    pl->bb.maxM = pl->maxG;
+
+    fo::RefineBuffers &r = pl->rb;
+    r.pairs = pl->sb.pairs;
+    r.groups = pl->sb.groups;
+    r.slot2orig = pl->sb.slot2orig;
+    r.cand2pair = (const int *)P(o_c2p);
+    r.xa = pl->sb.xa;
+    r.xb = pl->sb.xb;
+    r.grid = P(o_grid);
+    r.overlap_max = (double *)P(o_omax);
+    r.peaks = (double *)P(o_peaks);
+    r.npeaks = (int *)P(o_npk);
+    r.pstatus = (int *)P(o_pst);
+    r.lap = (unsigned char *)P(o_lap);
+    r.cdist = (double *)P(o_cdist);
+    r.cR = (double *)P(o_cR);
+    r.cdisp = (double *)P(o_cdisp);
+    r.cxyz = (double *)P(o_cxyz);
+    r.cperm = (int *)P(o_cperm);
+    r.cniter = (int *)P(o_cnit);
+    r.cstat = (int *)P(o_cst);
+    r.results = P(o_res);
+    r.aligned = (double *)P(o_al);
+    r.permbest = (int *)P(o_pb);
+    r.npairs = np;
+    r.ncand = nc;
+    r.maxG = pl->maxG;
+    r.maxn = pl->maxn;
+    pl->d_pstatus = r.pstatus;
+    pl->d_npeaks = r.npeaks;
+    return FO_OK;
+}
+
+fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
+                                 const double *pos1, const double *pos2, const int *perm,
+                                 const int *group_sizes, int index_base, fo_plan **out) {
+    if (!ctx || !out || npairs <= 0 || !pairs || !pos1 || !pos2 || !perm || !group_sizes)
+        return set_err(ctx, FO_ERR_BAD_ARGS, "null argument or npairs <= 0");
+    *out = nullptr;
+    cudaSetDevice(ctx->opts.device);
+    fo_plan *pl = new fo_plan();
+    pl->ctx = ctx;
+    pl->bulk = false;
+    pl->fp32 = ctx->opts.precision == FO_PREC_MIXED;
+    pl->npairs = npairs;
+    pl->index_base = index_base;
+    std::vector<int> slot2orig, slot2pair, cand2pair;
+    std::vector<double> hpos1, hpos2;
+    std::vector<int> bws;
+    long long ylm_n = 0, w_n = 0, coef_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
+    int atom0 = 0, cand0 = 0;
+    for (int i = 0; i < npairs; ++i) {
+        const fo_cluster_pair &q = pairs[i];
+        const int n = q.natoms, L = q.jmax;
+        if (n < 1 || n > kMaxAtoms) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: natoms %d outside [1,%d]", i, n, kMaxAtoms); }
+        if (L < 0 || L > kMaxJmax) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: jmax %d outside [0,%d]", i, L, kMaxJmax); }
+        if (q.nrot < 1 || q.nrot > kMaxNrot) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: nrot %d outside [1,%d]", i, q.nrot, kMaxNrot); }
+        if (!(q.sigma == q.sigma)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: sigma is NaN", i); }
+        std::vector<int> s2o(n);
+        fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
+                                   index_base, s2o.data());
+        if (s) { delete pl; return s; }
+        for (int k = 0; k < 3 * n; ++k) {
+            double a = pos1[3 * q.coord_off + k], b = pos2[3 * q.coord_off + k];
+            if (!std::isfinite(a) || !std::isfinite(b)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: non-finite coordinate", i); }
+        }
+        fo::PairDev P{};
+        P.n = n;
+        P.ngroups = q.ngroups;
+        P.group0 = (int)pl->hg.size();
+        P.L = L;
+        P.G = 2 * (L + 1);
+        P.nrot = q.nrot;
+        P.norient = q.invert ? 2 : 1;
+        P.atom0 = atom0;
+        P.cand0 = cand0;
+        P.bulk = 0;
+        P.ylm0 = ylm_n;
+        P.coef0 = coef_n;
+        P.grid0 = grid_n;
+        P.candatom0 = candatom;
+        P.sigma = q.sigma;
+        int maxg = 0, off = 0;
+        for (int g = 0; g < q.ngroups; ++g) {
+            int gn = group_sizes[q.group_off + g];
+            fo::GroupDev G{};
+            G.pair = i;
+            G.slot0 = atom0 + off;
+            G.n = gn;
+            G.m = std::min(gn, fo::kMaxNei);
+            G.w0 = w_n;
+            w_n += (long long)(L + 1) * gn * gn;
+            off += gn;
+            maxg = std::max(maxg, gn);
+            pl->maxgroup = std::max(pl->maxgroup, gn);
+            pl->hg.push_back(G);
+        }
+        P.lapstride = fo::lap_bytes_host(maxg);
+        P.lap0 = lap_total;
+        lap_total += (long long)P.norient * P.nrot * P.lapstride;
+        pl->hp.push_back(P);
+        pl->caller_off.push_back(q.coord_off);
+        for (int s = 0; s < n; ++s) {
+            slot2orig.push_back(s2o[s]);
+            slot2pair.push_back(i);
+        }
+        for (int c = 0; c < P.norient * P.nrot; ++c) cand2pair.push_back(i);
+        hpos1.insert(hpos1.end(), pos1 + 3 * q.coord_off, pos1 + 3 * (q.coord_off + n));
+        hpos2.insert(hpos2.end(), pos2 + 3 * q.coord_off, pos2 + 3 * (q.coord_off + n));
+        ylm_n += (long long)n * (L + 1) * (L + 1);
+        coef_n += (long long)(L + 1) * (2 * L + 1) * (2 * L + 1);
+        grid_n += (long long)P.norient * P.G * P.G * P.G;
+        candatom += (long long)P.norient * P.nrot * n;
+        atom0 += n;
+        cand0 += P.norient * P.nrot;
+        pl->maxL = std::max(pl->maxL, L);
+        pl->maxG = std::max(pl->maxG, P.G);
+        pl->maxn = std::max(pl->maxn, n);
+        bws.push_back(L + 1);
+    }
+    pl->nslots = atom0;
+    pl->ncand = cand0;
+    pl->ngroups = (int)pl->hg.size();
+    std::sort(bws.begin(), bws.end());
+    bws.erase(std::unique(bws.begin(), bws.end()), bws.end());
+    fo_status s = ensure_dtabs(ctx, bws);
+    if (s) { delete pl; return s; }
+    s = plan_common_alloc(ctx, pl, hpos1.data(), hpos2.data(), slot2orig, slot2pair, cand2pair,
+                          ylm_n, w_n, coef_n, grid_n, 0, lap_total);
+    if (s) { fo_plan_destroy(pl); return s; }
+    pl->sb.dtab = pl->fp32 ? (const void *const *)ctx->d_dtab32 : (const void *const *)ctx->d_dtab64;
+    *out = pl;
+    return FO_OK;
+}
+
+fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs, const double *pos1,
+                              const double *pos2, const int *perm, const int *group_sizes,
+                              int index_base, fo_plan **out) {
+    if (!ctx || !out || npairs <= 0 || !pairs || !pos1 || !pos2 || !perm || !group_sizes)
+        return set_err(ctx, FO_ERR_BAD_ARGS, "null argument or npairs <= 0");
+    *out = nullptr;
+    cudaSetDevice(ctx->opts.device);
+    fo_plan *pl = new fo_plan();
+    pl->ctx = ctx;
+    pl->bulk = true;
+    pl->fp32 = ctx->opts.precision == FO_PREC_MIXED;
+    pl->npairs = npairs;
+    pl->index_base = index_base;
+    std::vector<int> slot2orig, slot2pair, cand2pair;
+    std::vector<double> hpos1, hpos2;
+    long long fgrid_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
+    int atom0 = 0, cand0 = 0;
+    for (int i = 0; i < npairs; ++i) {
+        const fo_bulk_pair &q = pairs[i];
+        const int n = q.natoms;
+        if (n < 1 || n > kMaxAtoms) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: natoms %d outside [1,%d]", i, n, kMaxAtoms); }
+        for (int k = 0; k < 3; ++k)
+            if (!(q.box[k] > 0.0) || !std::isfinite(q.box[k])) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: box lengths must be positive", i); }
+        int K = q.nwave > 0 ? q.nwave : (int)std::ceil(1.3 * std::cbrt((double)n));
+        int M = q.nfspace > 0 ? q.nfspace : fastlen(4 * K + 3);
+        int nd = q.ndisps > 0 ? q.ndisps : 10;
+        double sg = q.sigma > 0 ? q.sigma : std::cbrt(q.box[0] * q.box[1] * q.box[2] / n) / 3.0;
+        if (M < 2 * K + 1 || M > kMaxM) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: nfspace %d must lie in [2K+1, %d]", i, M, kMaxM); }
+        if (nd > kMaxNrot) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: ndisps %d > %d", i, nd, kMaxNrot); }
+        std::vector<int> s2o(n);
+        fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
+                                   index_base, s2o.data());
+        if (s) { delete pl; return s; }
+        for (int k = 0; k < 3 * n; ++k) {
+            double a = pos1[3 * q.coord_off + k], b = pos2[3 * q.coord_off + k];
+            if (!std::isfinite(a) || !std::isfinite(b)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: non-finite coordinate", i); }
+        }
+        fo::PairDev P{};
+        P.n = n;
+        P.ngroups = q.ngroups;
+        P.group0 = (int)pl->hg.size();
+        P.L = K;
+        P.G = M;
+        P.nrot = nd;
+        P.norient = 1;
+        P.atom0 = atom0;
+        P.cand0 = cand0;
+        P.bulk = 1;
+        P.coef0 = fgrid_n;
+        P.grid0 = grid_n;
+        P.candatom0 = candatom;
+        P.sigma = sg;
+        for (int k = 0; k < 3; ++k) P.box[k] = q.box[k];
+        int maxg = 0, off = 0;
+        for (int g = 0; g < q.ngroups; ++g) {
+            int gn = group_sizes[q.group_off + g];
+            fo::GroupDev G{};
+            G.pair = i;
+            G.slot0 = atom0 + off;
+            G.n = gn;
+            G.m = std::min(gn, fo::kMaxNei);
+            off += gn;
+            maxg = std::max(maxg, gn);
+            pl->hg.push_back(G);
+        }
+        P.lapstride = fo::lap_bytes_host(maxg);
+        P.lap0 = lap_total;
+        lap_total += (long long)P.nrot * P.lapstride;
+        pl->hp.push_back(P);
+        pl->caller_off.push_back(q.coord_off);
+        for (int s = 0; s < n; ++s) {
+            slot2orig.push_back(s2o[s]);
+            slot2pair.push_back(i);
+        }
+        for (int c = 0; c < P.nrot; ++c) cand2pair.push_back(i);
+        hpos1.insert(hpos1.end(), pos1 + 3 * q.coord_off, pos1 + 3 * (q.coord_off + n));
+        hpos2.insert(hpos2.end(), pos2 + 3 * q.coord_off, pos2 + 3 * (q.coord_off + n));
+        fgrid_n += (long long)M * M * M;
+        grid_n += (long long)M * M * M;
+        candatom += (long long)P.nrot * n;
+        atom0 += n;
+        cand0 += P.nrot;
+        pl->maxL = std::max(pl->maxL, K);
+        pl->maxG = std::max(pl->maxG, M);
+        pl->maxn = std::max(pl->maxn, n);
+    }
+    pl->nslots = atom0;
+    pl->ncand = cand0;
+    pl->ngroups = (int)pl->hg.size();
+    fo_status s = plan_common_alloc(ctx, pl, hpos1.data(), hpos2.data(), slot2orig, slot2pair,
+                                    cand2pair, 0, 0, 0, grid_n, fgrid_n, lap_total);
+    if (s) { fo_plan_destroy(pl); return s; }
+    *out = pl;
+    return FO_OK;
+}
+
+fo_status fo_plan_run(fo_plan *pl) {
+    if (!pl) return FO_ERR_BAD_ARGS;
+    fo_ctx *ctx = pl->ctx;
+    cudaSetDevice(ctx->opts.device);
+    cudaStream_t st = ctx->stream;
+    for (auto e : pl->evs) cudaEventDestroy(e);
+    pl->evs.clear();
+    pl->ev_kid.clear();
+    rec_event(pl, -1);
+    cudaMemsetAsync(pl->d_pstatus, 0, pl->npairs * sizeof(int), st);
+    cudaMemsetAsync(pl->d_npeaks, 0, 2 * pl->npairs * sizeof(int), st);
+    if (!pl->bulk) {
+        cudaMemsetAsync(pl->d_coef, 0, pl->coef_bytes, st);
+        rec_event(pl, K_MEMSET);
+        fo::launch_sph_center(pl->sb, st);     rec_event(pl, K_CENTER);
+        fo::launch_sph_ylm(pl->sb, pl->fp32, st); rec_event(pl, K_YLM);
+        fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st); rec_event(pl, K_RADIAL);
+        fo::launch_sph_coeff(pl->sb, pl->fp32, st); rec_event(pl, K_COEFF);
+        fo::launch_isoft(pl->sb, pl->fp32, st);    rec_event(pl, K_ISOFT);
+    } else {
+        cudaMemsetAsync(pl->d_fgrid, 0, pl->fgrid_bytes, st);
+        rec_event(pl, K_MEMSET);
+        fo::launch_bulk_prep(pl->bb, st);          rec_event(pl, K_BPREP);
+        fo::launch_bulk_sf(pl->bb, pl->fp32, st);  rec_event(pl, K_BSF);
+        fo::launch_bulk_fft(pl->bb, pl->fp32, st); rec_event(pl, K_BFFT);
+    }
+    fo::launch_findpeaks(pl->rb, pl->fp32, st); rec_event(pl, K_PEAKS);
+    fo::launch_refine(pl->rb, st);              rec_event(pl, K_REFINE);
+    fo::launch_select(pl->rb, st);              rec_event(pl, K_SELECT);
+    return cuda_check(ctx, cudaGetLastError(), "kernel launch");
+}
+
+fo_status fo_plan_wait(fo_plan *pl) {
+    if (!pl) return FO_ERR_BAD_ARGS;
+    fo_ctx *ctx = pl->ctx;
+    fo_status s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "pipeline");
+    if (s) return s;
+    if (ctx->opts.profile && pl->evs.size() > 1) {
+        for (size_t i = 1; i < pl->evs.size(); ++i) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, pl->evs[i - 1], pl->evs[i]);
+            int k = pl->ev_kid[i];
+            if (k >= 0 && k < kNumKernels) {
+                ctx->prof_ms[k] += ms;
+                ctx->prof_n[k] += 1;
+            }
+        }
+    }
+    return FO_OK;
+}
+
+fo_status fo_plan_results(fo_plan *pl, double *aligned, int *permbest, fo_pair_result *results) {
+    if (!pl) return FO_ERR_BAD_ARGS;
+    fo_ctx *ctx = pl->ctx;
+    const int np = pl->npairs, ns = pl->nslots;
+    std::vector<fo_pair_result> res(np);
+    std::vector<double> al(aligned ? 3 * (size_t)ns : 0);
+    std::vector<int> pb(permbest ? ns : 0);
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(res.data(), pl->rb.results, np * sizeof(fo_pair_result), cudaMemcpyDeviceToHost, st);
+    if (aligned) cudaMemcpyAsync(al.data(), pl->rb.aligned, al.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (permbest) cudaMemcpyAsync(pb.data(), pl->rb.permbest, pb.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
+    fo_status s = cuda_check(ctx, cudaStreamSynchronize(st), "result download");
+    if (s) return s;
+    int worst = FO_OK;
+    for (int i = 0; i < np; ++i) {
+        const fo::PairDev &P = pl->hp[i];
+        if (results) results[i] = res[i];
+        if (res[i].status > worst) worst = res[i].status;
+        long long co = pl->caller_off[i];
+        if (aligned) memcpy(aligned + 3 * co, al.data() + 3 * (size_t)P.atom0, 3 * (size_t)P.n * sizeof(double));
+        if (permbest)
+            for (int j = 0; j < P.n; ++j) permbest[co + j] = pb[P.atom0 + j] + pl->index_base;
+    }
+    (void)worst;
+    return FO_OK;
+}
+
+size_t fo_plan_device_bytes(const fo_plan *pl) { return pl ? pl->dbytes : 0; }
+
+void fo_plan_destroy(fo_plan *pl) {
+    if (!pl) return;
+    cudaSetDevice(pl->ctx->opts.device);
+    cudaStreamSynchronize(pl->ctx->stream);
+    for (auto e : pl->evs) cudaEventDestroy(e);
+    cudaFree(pl->dmem);
+    delete pl;
+}
+
+static fo_status run_batch(fo_ctx *ctx, fo_plan *pl, double *aligned, int *permbest,
+                           fo_pair_result *results) {
+    fo_status s = fo_plan_run(pl);
+    if (!s) s = fo_plan_wait(pl);
+    if (!s) s = fo_plan_results(pl, aligned, permbest, results);
+    fo_plan_destroy(pl);
+    (void)ctx;
+    return s;
+}
+
+fo_status fo_cluster_align_batch(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
+                                 const double *pos1, const double *pos2, const int *perm,
+                                 const int *group_sizes, int index_base, double *aligned,
+                                 int *permbest, fo_pair_result *results) {
+    fo_plan *pl = nullptr;
+    fo_status s = fo_cluster_plan_create(ctx, npairs, pairs, pos1, pos2, perm, group_sizes, index_base, &pl);
+    if (s) return s;
+    return run_batch(ctx, pl, aligned, permbest, results);
+}
+
+fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs, const double *pos1,
+                              const double *pos2, const int *perm, const int *group_sizes,
+                              int index_base, double *aligned, int *permbest, fo_pair_result *results) {
+    fo_plan *pl = nullptr;
+    fo_status s = fo_bulk_plan_create(ctx, npairs, pairs, pos1, pos2, perm, group_sizes, index_base, &pl);
+    if (s) return s;
+    return run_batch(ctx, pl, aligned, permbest, results);
+}
+
+// ---------------------------------------------------------------------------
+// Fortran-style entry points
+fo_status fo_setperm(fo_ctx *ctx, int natoms, const int *permgroup, const int *npermsize, int npermgroup) {
+    if (!ctx || natoms < 1 || !permgroup || !npermsize || npermgroup < 1) return FO_ERR_BAD_ARGS;
+    long long tot = 0;
+    for (int g = 0; g < npermgroup; ++g) tot += npermsize[g];
+    ctx->permgroup.assign(permgroup, permgroup + tot);
+    ctx->npermsize.assign(npermsize, npermsize + npermgroup);
+    ctx->perm_natoms = natoms;
+    return FO_OK;
+}
+
+fo_status fo_get_bestperm(const fo_ctx *ctx, int *bestperm) {
+    if (!ctx || !bestperm || ctx->bestperm.empty()) return FO_ERR_BAD_ARGS;
+    memcpy(bestperm, ctx->bestperm.data(), ctx->bestperm.size() * sizeof(int));
+    return FO_OK;
+}
+
+static void current_groups(fo_ctx *ctx, int natoms, std::vector<int> &perm, std::vector<int> &sizes) {
+    if (ctx->perm_natoms == natoms && !ctx->permgroup.empty()) {
+        perm = ctx->permgroup;
+        sizes = ctx->npermsize;
+    } else {
+        perm.resize(natoms);
+        for (int i = 0; i < natoms; ++i) perm[i] = i + 1;
+        sizes.assign(1, natoms);
+    }
+}
+
+fo_status fo_cluster_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms, int debug, int l,
+                           double *kwidth, int nrotations, int perminvopt, double *distance,
+                           double *dist2, double *rmatbest) {
+    (void)debug;
+    if (!ctx || !coordsb || !coordsa || natoms < 1 || !kwidth) return FO_ERR_BAD_ARGS;
+    std::vector<int> perm, sizes;
+    current_groups(ctx, natoms, perm, sizes);
+    fo_cluster_pair q{};
+    q.natoms = natoms;
+    q.ngroups = (int)sizes.size();
+    q.jmax = l;
+    q.nrot = nrotations;
+    q.invert = perminvopt ? 1 : 0;
+    q.sigma = *kwidth;
+    std::vector<double> al(3 * (size_t)natoms);
+    std::vector<int> pb(natoms);
+    fo_pair_result r{};
+    fo_status s = fo_cluster_align_batch(ctx, 1, &q, coordsb, coordsa, perm.data(), sizes.data(), 1,
+                                         al.data(), pb.data(), &r);
+    if (s) return s;
+    if (r.status) return (fo_status)r.status;
+    double cb[3] = {0, 0, 0};
+    for (int j = 0; j < natoms; ++j)
+        for (int k = 0; k < 3; ++k) cb[k] += coordsb[3 * j + k];
+    for (int j = 0; j < natoms; ++j)
+        for (int k = 0; k < 3; ++k) coordsb[3 * j + k] -= cb[k] / natoms;
+    memcpy(coordsa, al.data(), al.size() * sizeof(double));
+    *kwidth = r.sigma;
+    if (distance) *distance = r.dist;
+    if (dist2) *dist2 = r.dist * r.dist;
+    if (rmatbest)
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) rmatbest[i + 3 * j] = r.rmat[3 * i + j];
+    ctx->bestperm = pb;
+    return FO_OK;
+}
+
+fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms, int debug, double boxlx,
+                        double boxly, double boxlz, double kwidth, int ndisplacements, int nwave,
+                        int nfspace, double *distance, double *dist2) {
+    (void)debug;
+    if (!ctx || !coordsb || !coordsa || natoms < 1) return FO_ERR_BAD_ARGS;
+    std::vector<int> perm, sizes;
+    current_groups(ctx, natoms, perm, sizes);
+    fo_bulk_pair q{};
+    q.natoms = natoms;
+    q.ngroups = (int)sizes.size();
+    q.nwave = nwave;
+    q.nfspace = nfspace;
+    q.ndisps = ndisplacements;
+    q.sigma = kwidth;
+    q.box[0] = boxlx;
+    q.box[1] = boxly;
+    q.box[2] = boxlz;
+    std::vector<double> al(3 * (size_t)natoms);
+    std::vector<int> pb(natoms);
+    fo_pair_result r{};
+    fo_status s = fo_bulk_align_batch(ctx, 1, &q, coordsb, coordsa, perm.data(), sizes.data(), 1,
+                                      al.data(), pb.data(), &r);
+    if (s) return s;
+    if (r.status) return (fo_status)r.status;
+    memcpy(coordsa, al.data(), al.size() * sizeof(double));
+    if (distance) *distance = r.dist;
+    if (dist2) *dist2 = r.dist * r.dist;
+    ctx->bestperm = pb;
+    return FO_OK;
+}
+
+fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz, double *kernelwidth,
+                               int *nwave, int *nfspace) {
+    if (natoms < 1 || !kernelwidth || !nwave || !nfspace) return FO_ERR_BAD_ARGS;
+    double kw = std::cbrt(boxlx * boxly * boxlz / natoms) / 3.0;
+    double maxk = 1.5 / kw;
+    int nw = (int)std::ceil(2 * 3.14159265359 / std::min(boxlx, std::min(boxly, boxlz)) * maxk);
+    *kernelwidth = kw;
+    *nwave = nw;
+    *nfspace = fastlen(4 * nw + 3);
+    return FO_OK;
+}
+
+int fo_profile_kernels(const fo_ctx *ctx, const char **names, double *ms_total, int *launches, int cap) {
+    if (!ctx) return 0;
+    int k = 0;
+    for (int i = 0; i < kNumKernels && k < cap; ++i) {
+        if (ctx->prof_n[i] == 0) continue;
+        if (names) names[k] = kKernelNames[i];
+        if (ms_total) ms_total[k] = ctx->prof_ms[i];
+        if (launches) launches[k] = ctx->prof_n[i];
+        ++k;
+    }
+    return k;
+}
+
+void fo_profile_reset(fo_ctx *ctx) {
+    if (!ctx) return;
+    for (int i = 0; i < kNumKernels; ++i) { ctx->prof_ms[i] = 0; ctx->prof_n[i] = 0; }
+}
+
+}  // extern "C"

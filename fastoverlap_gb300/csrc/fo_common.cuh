@@ -1,0 +1,252 @@
+// fo_common.cuh -- shared device/host definitions of the GB300 FASTOVERLAP
+// library: plan descriptors, complex helpers, reductions, the shared-memory
+// Stockham FFT and small dense linear algebra used by several kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#ifndef FO_PI
+#define FO_PI 3.141592653589793238462643383279502884
+#endif
+
+namespace fo {
+
+// ---------------------------------------------------------------------------
+// Plan descriptors (device-resident, built on the host).
+// A "slot" is an atom position after the atoms of a pair are reordered so that
+// each permutation group is contiguous; slot s of pair p holds original atom
+// perm[s] (the concatenated group list is exactly the slot -> atom map).
+struct PairDev {
+    int n;          // atoms
+    int ngroups;    // permutation groups
+    int group0;     // first GroupDev of this pair
+    int L;          // cluster: Jmax; bulk: nwave K
+    int G;          // cluster: 2(L+1); bulk: nfspace M
+    int nrot;       // candidate slots per orientation
+    int norient;    // 2 when the inverted copy is aligned too, else 1
+    int atom0;      // first slot (global)
+    int cand0;      // first candidate (global), norient*nrot candidates
+    int bulk;       // 1 periodic, 0 cluster
+    long long ylm0;      // complex offset into the Y_lm arrays
+    long long coef0;     // complex offset: cluster coefficients / bulk F grid
+    long long grid0;     // offset into the real overlap grids (norient * G^3)
+    long long candatom0; // offset of per-atom candidate outputs
+    long long lap0;      // offset (bytes) of this pair's LAP scratch
+    long long lapstride; // LAP scratch bytes per candidate
+    double sigma;
+    double box[3];
+};
+
+struct GroupDev {
+    int pair;
+    int slot0;      // first slot (global)
+    int n;          // atoms in the group
+    int m;          // neighbours kept per row: min(n, 60)
+    long long w0;   // offset of the radial weight block [(L+1)][n][n]
+};
+
+// status codes shared with the C ABI (fastoverlap_gb300.h)
+enum : int {
+    ST_OK = 0, ST_BAD_ARGS = 1, ST_NO_PEAKS = 2, ST_LAP_FAILED = 3, ST_TIMEOUT = 4
+};
+
+constexpr int kMaxNei = 60;          // PMAXNEI, alignutils.f90:79
+constexpr double kPScale = 1.0e6;    // PSCALE, alignutils.f90:80
+constexpr int kMaxTries = 20;        // MAXIMUMTRIES, alignutils.f90:81
+constexpr long long kBigInt = 1000000000000LL;  // BIGINT, alignutils.f90:1007
+
+// ---------------------------------------------------------------------------
+// complex helpers over double2 / float2
+template <typename T> struct cplx;
+template <> struct cplx<double> { using type = double2; };
+template <> struct cplx<float> { using type = float2; };
+
+template <typename T2> __host__ __device__ inline T2 mk2(double a, double b) {
+    T2 r; r.x = a; r.y = b; return r;
+}
+template <typename T2> __device__ inline T2 cmul(T2 a, T2 b) {
+    T2 r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename T2> __device__ inline T2 cadd(T2 a, T2 b) {
+    T2 r; r.x = a.x + b.x; r.y = a.y + b.y; return r;
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+template <typename T> __device__ inline T warp_sum(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of K values per thread; result broadcast to every thread.
+// scratch: >= 32*K elements of T in shared memory.  All threads must call.
+template <typename T, int K>
+__device__ inline void block_sum(T (&v)[K], T *scratch) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) scratch[wid * K + k] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        T s = 0;
+        for (int w = 0; w < nw; ++w) s += scratch[w * K + k];
+        v[k] = s;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Stockham autosort FFT over a batch of lines held in shared memory.
+// Element e of line l lives at buf[l*lstride + e*estride].  Radix 2,3,4,5
+// passes; lengths with another prime factor use a direct DFT.  sign = -1 is
+// the forward transform, +1 the unnormalised backward one.  tw[t] holds
+// exp(+2 pi i t/n).  Returns the buffer (x or y) that holds the result.
+// All threads of the block must call it.
+__host__ __device__ inline int fft_factor(int n, int *rad) {
+    int k = 0;
+    while (n % 4 == 0) { rad[k++] = 4; n /= 4; }
+    while (n % 2 == 0) { rad[k++] = 2; n /= 2; }
+    while (n % 3 == 0) { rad[k++] = 3; n /= 3; }
+    while (n % 5 == 0) { rad[k++] = 5; n /= 5; }
+    if (n != 1) return -1;
+    return k;
+}
+
+template <typename T2>
+__device__ inline T2 tw_get(const T2 *tw, int n, long long e, int sign) {
+    int t = (int)(((e % n) + n) % n);
+    T2 w = tw[t];
+    if (sign < 0) w.y = -w.y;
+    return w;
+}
+
+template <typename T2>
+__device__ T2 *fft_lines(T2 *x, T2 *y, int n, int nlines, int lstride, int estride, int sign,
+                         const T2 *tw) {
+    int rad[24];
+    int nr = fft_factor(n, rad);
+    if (nr < 0) {  // direct DFT
+        for (int t = threadIdx.x; t < nlines * n; t += blockDim.x) {
+            int l = t / n, q = t % n;
+            const T2 *xl = x + (long long)l * lstride;
+            T2 acc = mk2<T2>(0, 0);
+            for (int j = 0; j < n; ++j)
+                acc = cadd(acc, cmul(xl[(long long)j * estride], tw_get(tw, n, (long long)j * q, sign)));
+            y[(long long)l * lstride + (long long)q * estride] = acc;
+        }
+        __syncthreads();
+        return y;
+    }
+    int Ns = 1;
+    for (int s = 0; s < nr; ++s) {
+        const int p = rad[s], nb = n / p, tstep = n / (Ns * p);
+        for (int t = threadIdx.x; t < nlines * nb; t += blockDim.x) {
+            int l = t / nb, j = t % nb, k = j % Ns;
+            const T2 *xl = x + (long long)l * lstride;
+            T2 *yl = y + (long long)l * lstride;
+            T2 v[5], o[5];
+            for (int r = 0; r < p; ++r) {
+                T2 a = xl[(long long)(j + r * nb) * estride];
+                v[r] = (r == 0 || k == 0) ? a : cmul(a, tw_get(tw, n, (long long)k * r * tstep, sign));
+            }
+            for (int q = 0; q < p; ++q) {
+                T2 acc = v[0];
+                for (int r = 1; r < p; ++r)
+                    acc = cadd(acc, cmul(v[r], tw_get(tw, n, (long long)r * q * (n / p), sign)));
+                o[q] = acc;
+            }
+            int idxD = (j / Ns) * Ns * p + k;
+            for (int q = 0; q < p; ++q) yl[(long long)(idxD + q * Ns) * estride] = o[q];
+        }
+        __syncthreads();
+        T2 *tmp = x; x = y; y = tmp;
+        Ns *= p;
+    }
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// Euler matrix of EULERM (fastclusters.f90:990-1016), row-major.
+__host__ __device__ inline void euler_matrix(double a, double b, double g, double *R) {
+    double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cg = cos(g), sg = sin(g);
+    R[0] = cg * cb * ca - sg * sa;  R[1] = sg * cb * ca + cg * sa;  R[2] = sb * ca;
+    R[3] = -cg * cb * sa - sg * ca; R[4] = -sg * cb * sa + cg * ca; R[5] = -sb * sa;
+    R[6] = -cg * sb;                R[7] = -sg * sb;                R[8] = cb;
+}
+
+__host__ __device__ inline void matmul3(const double *X, const double *Y, double *Z) {
+    double T[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            T[3 * i + j] = X[3 * i] * Y[j] + X[3 * i + 1] * Y[3 + j] + X[3 * i + 2] * Y[6 + j];
+    for (int i = 0; i < 9; ++i) Z[i] = T[i];
+}
+
+// Symmetric 4x4 eigenproblem by cyclic Jacobi rotations (Golub & Van Loan
+// 8.5); replaces LAPACK DSYEV in FINDROTATION (alignutils.f90:346).
+__host__ __device__ inline void jacobi4(double a[4][4], double w[4], double V[4][4]) {
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) off += a[p][q] * a[p][q];
+        if (off == 0.0) break;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) {
+                if (a[p][q] == 0.0) continue;
+                double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 4; ++k) {
+                    double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < 4; ++i) w[i] = a[i][i];
+}
+
+// Quaternion rotation from the 10 unique Kearsley sums (FINDROTATION,
+// alignutils.f90:323-377).  q = {Q11,Q12,Q13,Q14,Q22,Q23,Q24,Q33,Q34,Q44}.
+__host__ __device__ inline double kearsley_rotation(const double *q, double *R) {
+    double Q[4][4] = {{q[0], q[1], q[2], q[3]},
+                      {q[1], q[4], q[5], q[6]},
+                      {q[2], q[5], q[7], q[8]},
+                      {q[3], q[6], q[8], q[9]}};
+    double w[4], V[4][4];
+    jacobi4(Q, w, V);
+    int jmin = 0;
+    double minv = 1.0e100;
+    for (int j = 0; j < 4; ++j)
+        if (w[j] < minv) { minv = w[j]; jmin = j; }
+    if (minv < 0.0) minv = (fabs(minv) < 1e-6) ? 0.0 : -minv;
+    double q1 = V[0][jmin], q2 = V[1][jmin], q3 = V[2][jmin], q4 = V[3][jmin];
+    R[0] = q1 * q1 + q2 * q2 - q3 * q3 - q4 * q4;
+    R[1] = 2 * (q2 * q3 + q1 * q4);
+    R[2] = 2 * (q2 * q4 - q1 * q3);
+    R[3] = 2 * (q2 * q3 - q1 * q4);
+    R[4] = q1 * q1 + q3 * q3 - q2 * q2 - q4 * q4;
+    R[5] = 2 * (q3 * q4 + q1 * q2);
+    R[6] = 2 * (q2 * q4 + q1 * q3);
+    R[7] = 2 * (q3 * q4 - q1 * q2);
+    R[8] = q1 * q1 + q4 * q4 - q2 * q2 - q3 * q3;
+    return sqrt(minv);
+}
+
+}  // namespace fo

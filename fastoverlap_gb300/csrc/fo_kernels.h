@@ -1,0 +1,74 @@
+// fo_kernels.h -- host-side launch wrappers exported by the kernel files and
+// used by the C-ABI layer (fo_api.cu).  All launches are asynchronous on the
+// given stream.
+#pragma once
+#include <cuda_runtime.h>
+#include "fo_common.cuh"
+
+namespace fo {
+
+struct SphBuffers {
+    const PairDev *pairs;
+    const GroupDev *groups;
+    const int *slot2orig;   // per slot: original atom index within the pair
+    const int *slot2pair;   // per slot
+    const double *pos1, *pos2;  // packed original-order inputs (3 per atom)
+    double *xa, *xb;        // slot-ordered centred coordinates (3 per slot)
+    double *ra, *rb;        // per slot radii
+    void *ylmA, *ylmB;      // complex T per (slot, lm)
+    void *W;                // radial weights (T)
+    void *coef;             // complex T coefficients (ilmm layout)
+    void *grid;             // real T overlap grids
+    const void *const *dtab;  // per bandwidth: Wigner table (T), layout [k][m1][m2][l]
+    int npairs, ngroups, nslots, maxL, maxG, maxgroup;
+};
+
+// spherical stages
+void launch_sph_center(const SphBuffers &b, cudaStream_t s);
+void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s);
+void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s);
+void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s);
+void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s);
+void launch_wigner_table(int bw, double *d64, float *d32, cudaStream_t s);
+
+// periodic stages
+struct BulkBuffers {
+    const PairDev *pairs;
+    const GroupDev *groups;
+    const int *slot2orig;
+    const double *pos1, *pos2;
+    double *xa, *xb;
+    void *fgrid;            // complex T, M^3 per pair
+    void *grid;             // real T, M^3 per pair
+    int npairs, maxK, maxM;
+};
+void launch_bulk_prep(const BulkBuffers &b, cudaStream_t s);
+void launch_bulk_sf(const BulkBuffers &b, bool fp32, cudaStream_t s);
+void launch_bulk_fft(const BulkBuffers &b, bool fp32, cudaStream_t s);
+
+// peaks and refinement (shared)
+struct RefineBuffers {
+    const PairDev *pairs;
+    const GroupDev *groups;
+    const int *slot2orig;
+    const int *cand2pair;
+    const double *xa, *xb;
+    void *grid;             // real T, consumed (peaks are subtracted)
+    double *overlap_max;    // [pair][2]
+    double *peaks;          // [cand][3] 1-based fractional grid coordinates
+    int *npeaks;            // [pair][2]
+    int *pstatus;           // [pair]
+    unsigned char *lap;     // LAP scratch
+    double *cdist, *cR, *cdisp, *cxyz;
+    int *cperm, *cniter, *cstat;
+    // final outputs
+    void *results;          // fo_pair_result[npairs]
+    double *aligned;        // 3 per atom, original order
+    int *permbest;          // per atom, original order
+    int npairs, ncand, maxG, maxn;
+};
+void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s);
+void launch_refine(const RefineBuffers &b, cudaStream_t s);
+void launch_select(const RefineBuffers &b, cudaStream_t s);
+
+}  // namespace fo

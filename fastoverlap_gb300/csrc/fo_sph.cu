@@ -1,0 +1,446 @@
+// fo_sph.cu -- spherical (cluster) front end: centring, spherical harmonics,
+// radial pair weights, the SO(3) coefficient contraction, the Wigner-d table
+// and the inverse SO(3) transform onto the rotation grid.
+//
+// Reference behaviour (paths inside matthewghgriffiths/fastoverlap):
+//   centring                fastoverlap/f90/fastclusters.f90:173-185
+//   CHOOSE_KWIDTH           fastoverlap/f90/fastclusters.f90:1046-1101
+//   RYML (Y_lm)             fastoverlap/f90/fastclusters.f90:602-652
+//   SPHI (i_l)              fastoverlap/f90/fastutils.f90:1000-1096
+//   FOURIERCOEFFS           fastoverlap/f90/fastclusters.f90:868-916
+//   CALCWIGNERD             fastoverlap/f90/DSOFT.f90:121-195
+//   ISOFT + CALCOVERLAP     fastoverlap/f90/DSOFT.f90:265-329, fastclusters.f90:918-960
+#include "fo_common.cuh"
+#include "fo_kernels.h"
+
+namespace fo {
+
+// ---------------------------------------------------------------------------
+// Centre both structures and gather them into slot (group) order; choose the
+// Gaussian width when the caller passed sigma <= 0.  One block per pair.
+__global__ void k_sph_center(PairDev *pairs, const int *slot2orig, const double *pos1,
+                             const double *pos2, double *xa, double *xb) {
+    __shared__ double red[32 * 6];
+    const int p = blockIdx.x;
+    PairDev P = pairs[p];
+    const int n = P.n, base = P.atom0;
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int k = 0; k < 3; ++k) {
+            s[k] += pos2[3 * (base + i) + k];
+            s[3 + k] += pos1[3 * (base + i) + k];
+        }
+    block_sum<double, 6>(s, red);
+    if (P.sigma <= 0.0) {  // CHOOSE_KWIDTH: mean nearest-neighbour distance / 3
+        double acc[1] = {0.0};
+        for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
+            const double *X = (t < n) ? pos2 : pos1;
+            int i = (t < n) ? t : t - n;
+            double best = 1.0e10;
+            for (int j = 0; j < n; ++j) {
+                if (j == i) continue;
+                double dx = X[3 * (base + i)] - X[3 * (base + j)];
+                double dy = X[3 * (base + i) + 1] - X[3 * (base + j) + 1];
+                double dz = X[3 * (base + i) + 2] - X[3 * (base + j) + 2];
+                double d = sqrt(dx * dx + dy * dy + dz * dz);
+                if (d < best) best = d;
+            }
+            acc[0] += best;
+        }
+        block_sum<double, 1>(acc, red);
+        if (threadIdx.x == 0) pairs[p].sigma = acc[0] / (6.0 * n);
+    }
+    for (int sl = threadIdx.x; sl < n; sl += blockDim.x) {
+        int o = slot2orig[base + sl];
+        for (int k = 0; k < 3; ++k) {
+            xa[3 * (base + sl) + k] = pos2[3 * (base + o) + k] - s[k] / n;
+            xb[3 * (base + sl) + k] = pos1[3 * (base + o) + k] - s[3 + k] / n;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Orthonormal Y_lm (Condon-Shortley phase) for l <= L of every slot of both
+// structures; one thread per (slot, side).  Output per slot: (L+1)^2 complex
+// values at index l*l + l + m.  An atom at the origin gets theta = 0.
+template <typename T2>
+__global__ void k_sph_ylm(const PairDev *pairs, const int *slot2pair, const double *xa,
+                          const double *xb, double *ra, double *rb, T2 *ylmA, T2 *ylmB,
+                          int nslots) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * nslots) return;
+    const int side = t / nslots, slot = t % nslots;
+    const PairDev &P = pairs[slot2pair[slot]];
+    const int L = P.L;
+    const double *X = side ? xb : xa;
+    double x = X[3 * slot], y = X[3 * slot + 1], z = X[3 * slot + 2];
+    double r = sqrt(x * x + y * y + z * z);
+    double ct = 1.0, phi = 0.0;
+    if (r > 0.0) {
+        ct = fmin(1.0, fmax(-1.0, z / r));
+        phi = atan2(y, x);
+    }
+    double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    (side ? rb : ra)[slot] = r;
+    T2 *out = (side ? ylmB : ylmA) + P.ylm0 + (long long)(slot - P.atom0) * (L + 1) * (L + 1);
+    double pmm = 0.28209479177387814347;  // 1/sqrt(4 pi)
+    for (int m = 0; m <= L; ++m) {
+        if (m > 0) pmm = -sqrt((2.0 * m + 1.0) / (2.0 * m)) * st * pmm;
+        double sm, cm;
+        sincos(m * phi, &sm, &cm);
+        double sgn = (m & 1) ? -1.0 : 1.0;
+        double p2 = 0.0, p1 = pmm;
+        for (int l = m; l <= L; ++l) {
+            double pl;
+            if (l == m) pl = pmm;
+            else if (l == m + 1) pl = sqrt(2.0 * m + 3.0) * ct * pmm;
+            else {
+                double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+                double b = sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+                pl = a * (ct * p1 - b * p2);
+            }
+            if (l > m) { p2 = p1; p1 = pl; }
+            out[l * l + l + m] = mk2<T2>(pl * cm, pl * sm);
+            if (m > 0) out[l * l + l - m] = mk2<T2>(sgn * pl * cm, -sgn * pl * sm);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Radial pair weights of FOURIERCOEFFS:
+//   w_l(a,b) = 4 pi^{5/2} s^3 i_l(x) e^{-(r_a^2 + r_b^2)/4s^2},  x = r_a r_b / 2s^2
+// evaluated as 4 pi^{5/2} s^3 [e^{-x} i_l(x)] e^{-(r_a - r_b)^2/4s^2} so
+// nothing overflows.  e^{-x} i_l(x) comes from Miller's backward recurrence
+// i_{l-1} = i_{l+1} + (2l+1)/x i_l started at l = L + 10 + 0.8x (full FP64
+// accuracy for L <= 63) and normalised by e^{-x} i_0 = (1 - e^{-2x})/2x; for
+// x < 1e-6 the leading series terms are used.  Layout per group:
+// W[w0 + (l*n + b)*n + a].
+template <typename T>
+__global__ void k_sph_radial(const PairDev *pairs, const GroupDev *groups, const double *ra,
+                             const double *rb, T *W, int cutoff) {
+    const GroupDev g = groups[blockIdx.y];
+    const int n = g.n;
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * n) return;
+    const int b = (int)(idx / n), a = (int)(idx % n);
+    const PairDev &P = pairs[g.pair];
+    const int L = P.L;
+    const double s = P.sigma;
+    const double r1 = ra[g.slot0 + a], r2 = rb[g.slot0 + b];
+    T *out = W + g.w0 + (long long)b * n + a;
+    const long long lstride = (long long)n * n;
+    if (cutoff && !(fabs(r1 - r2) < 4.0 * s)) {
+        for (int l = 0; l <= L; ++l) out[l * lstride] = T(0);
+        return;
+    }
+    const double pre = 4.0 * 17.493418327624862 /* pi^2.5 */ * s * s * s *
+                       exp(-(r1 - r2) * (r1 - r2) / (4.0 * s * s));
+    const double x = r1 * r2 / (2.0 * s * s);
+    if (x < 1.0e-6) {
+        double t = exp(-x);
+        for (int l = 0; l <= L; ++l) {
+            if (l > 0) t *= x / (2.0 * l + 1.0);
+            out[l * lstride] = T(pre * t * (1.0 + x * x / (2.0 * (2.0 * l + 3.0))));
+        }
+        return;
+    }
+    if (x >= 1000.0 && x >= (double)L * L) {
+        // e^{-x} i_l(x) = (1/2x) sum_{k<=l} (l+k)!/(k!(l-k)!) (-1/2x)^k  (+ O(e^{-2x}));
+        // terms shrink at least by half when x >= l^2, so the sum is stable.
+        for (int l = 0; l <= L; ++l) {
+            double term = 1.0, sum = 1.0;
+            for (int k = 0; k < l; ++k) {
+                term *= -(double)(l + k + 1) * (double)(l - k) / ((k + 1.0) * 2.0 * x);
+                sum += term;
+            }
+            out[l * lstride] = T(pre * sum / (2.0 * x));
+        }
+        return;
+    }
+    double vals[64];
+    const int n0 = L + 10 + (int)(0.8 * x);
+    const double invx = 1.0 / x;
+    double fp1 = 0.0, f = 1.0;
+    for (int k = n0; k >= 1; --k) {
+        if (k <= L) vals[k] = f;
+        double fm1 = (2.0 * k + 1.0) * invx * f + fp1;
+        if (fabs(fm1) > 1.0e250) {
+            fm1 *= 1.0e-250;
+            f *= 1.0e-250;
+            for (int q = k; q <= L; ++q) vals[q] *= 1.0e-250;
+        }
+        fp1 = f;
+        f = fm1;
+    }
+    vals[0] = f;
+    const double s0 = -expm1(-2.0 * x) / (2.0 * x);
+    const double scale = pre * s0 / f;
+    for (int l = 0; l <= L; ++l) out[l * lstride] = T(vals[l] * scale);
+}
+
+// ---------------------------------------------------------------------------
+// Coefficient contraction, one block per (l, pair):
+//   I^l[m1][m2] = sum_groups sum_a ( sum_b YB_l[m1](b) W_l(b,a) ) conj(YA_l[m2](a))
+// as two tiled GEMMs through shared memory (a tiles of 32, b tiles of 32).
+// Written to the ilmm layout coef[coef0 + (l*W + m1 mod W)*W + m2 mod W].
+constexpr int kTA = 32, kTB = 32, kMaxWM = 63;
+
+template <typename T, typename T2>
+__global__ void __launch_bounds__(256) k_sph_coeff(const PairDev *pairs, const GroupDev *groups,
+                                                   const T2 *ylmA, const T2 *ylmB, const T *W,
+                                                   T2 *coef) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int l = blockIdx.x, p = blockIdx.y;
+    const PairDev P = pairs[p];
+    if (l > P.L) return;
+    const int WM = 2 * l + 1, L = P.L, LL = (L + 1) * (L + 1), Wc = 2 * L + 1;
+    T2 *sYB = (T2 *)smem_raw;              // [WM][kTB]
+    T2 *sP = sYB + kMaxWM * kTB;           // [WM][kTA]
+    T2 *sYA = sP + kMaxWM * kTA;           // [kTA][WM]
+    T *sW = (T *)(sYA + kTA * kMaxWM);     // [kTB][kTA]
+    const int tid = threadIdx.x, nt = blockDim.x;
+    T2 acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k] = mk2<T2>(0, 0);
+    for (int gi = 0; gi < P.ngroups; ++gi) {
+        const GroupDev g = groups[P.group0 + gi];
+        const int n = g.n;
+        const T *Wl = W + g.w0 + (long long)l * n * n;
+        const long long yb = P.ylm0 + (long long)(g.slot0 - P.atom0) * LL + l * l;
+        for (int a0 = 0; a0 < n; a0 += kTA) {
+            T2 pacc[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) pacc[k] = mk2<T2>(0, 0);
+            for (int b0 = 0; b0 < n; b0 += kTB) {
+                for (int t = tid; t < WM * kTB; t += nt) {
+                    int m1 = t / kTB, bb = t % kTB;
+                    sYB[m1 * kTB + bb] = (b0 + bb < n) ? ylmB[yb + (long long)(b0 + bb) * LL + m1] : mk2<T2>(0, 0);
+                }
+                for (int t = tid; t < kTB * kTA; t += nt) {
+                    int bb = t / kTA, aa = t % kTA;
+                    sW[t] = (b0 + bb < n && a0 + aa < n) ? Wl[(long long)(b0 + bb) * n + a0 + aa] : T(0);
+                }
+                __syncthreads();
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    int o = tid + k * nt;
+                    if (o < WM * kTA) {
+                        int m1 = o / kTA, aa = o % kTA;
+                        T2 s = pacc[k];
+                        for (int bb = 0; bb < kTB; ++bb) {
+                            T2 y = sYB[m1 * kTB + bb];
+                            T w = sW[bb * kTA + aa];
+                            s.x += y.x * w;
+                            s.y += y.y * w;
+                        }
+                        pacc[k] = s;
+                    }
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                int o = tid + k * nt;
+                if (o < WM * kTA) sP[o] = pacc[k];
+            }
+            for (int t = tid; t < kTA * WM; t += nt) {
+                int aa = t / WM, m2 = t % WM;
+                sYA[t] = (a0 + aa < n) ? ylmA[yb + (long long)(a0 + aa) * LL + m2] : mk2<T2>(0, 0);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                int o = tid + k * nt;
+                if (o < WM * WM) {
+                    int m1 = o / WM, m2 = o % WM;
+                    T2 s = acc[k];
+                    for (int aa = 0; aa < kTA; ++aa) {
+                        T2 pv = sP[m1 * kTA + aa], ya = sYA[aa * WM + m2];
+                        // pv * conj(ya)
+                        s.x += pv.x * ya.x + pv.y * ya.y;
+                        s.y += pv.y * ya.x - pv.x * ya.y;
+                    }
+                    acc[k] = s;
+                }
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        int o = tid + k * nt;
+        if (o < WM * WM) {
+            int m1 = o / WM - l, m2 = o % WM - l;
+            int i1 = (m1 + Wc) % Wc, i2 = (m2 + Wc) % Wc;
+            coef[P.coef0 + ((long long)l * Wc + i1) * Wc + i2] = acc[k];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Normalised Wigner little-d table sqrt((2l+1)/2) d^l_{m1 m2}(beta_k),
+// beta_k = pi(2k+1)/(4 bw), by the Kostelec-Rockmore three-term recurrence
+// in l from the closed-form seed at l = max(|m1|,|m2|).  FP64 always.
+// Layout d[((k*W + m1i)*W + m2i)*bw + l], W = 2bw-1, entries below the seed 0.
+__global__ void k_wigner_table(int bw, double *d64, float *d32) {
+    const int W = 2 * bw - 1, G = 2 * bw;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G * W * W) return;
+    const int k = t / (W * W), i1 = (t / W) % W, i2 = t % W;
+    const int m1 = (i1 < bw) ? i1 : i1 - W, m2 = (i2 < bw) ? i2 : i2 - W;
+    const int l0 = max(abs(m1), abs(m2));
+    double *o64 = d64 + (long long)t * bw;
+    float *o32 = d32 ? d32 + (long long)t * bw : nullptr;
+    for (int l = 0; l < l0; ++l) {
+        o64[l] = 0.0;
+        if (o32) o32[l] = 0.f;
+    }
+    const double beta = FO_PI * (2.0 * k + 1.0) / (4.0 * bw);
+    double c = cos(beta / 2), s = sin(beta / 2), cb = cos(beta);
+    int M, pc, ps;
+    double sgn_s;
+    if (l0 == m1) { M = m2; pc = l0 + m2; ps = l0 - m2; sgn_s = -1; }
+    else if (l0 == -m1) { M = m2; pc = l0 - m2; ps = l0 + m2; sgn_s = 1; }
+    else if (l0 == m2) { M = m1; pc = l0 + m1; ps = l0 - m1; sgn_s = 1; }
+    else { M = m1; pc = l0 - m1; ps = l0 + m1; sgn_s = -1; }
+    double lf = lgamma(2.0 * l0 + 1.0) - lgamma((double)l0 + M + 1.0) - lgamma((double)l0 - M + 1.0);
+    double seed = sqrt((2.0 * l0 + 1.0) / 2.0 * exp(lf));
+    double sv = sgn_s * s;
+    for (int q = 0; q < pc; ++q) seed *= c;
+    for (int q = 0; q < ps; ++q) seed *= sv;
+    double prev = 0.0, cur = seed;
+    o64[l0] = cur;
+    if (o32) o32[l0] = (float)cur;
+    for (int l = l0; l <= bw - 2; ++l) {
+        double dl = l, a = 0.0, cc = 0.0;
+        double t5 = 1.0 / sqrt(((dl + 1) * (dl + 1) - (double)m1 * m1) * ((dl + 1) * (dl + 1) - (double)m2 * m2));
+        double bb = sqrt((2 * dl + 3) / (2 * dl + 1)) * (dl + 1) * (2 * dl + 1) * t5;
+        if (l > 0) {
+            a = sqrt((2 * dl + 3) / (2 * dl - 1)) * (dl + 1) / dl *
+                sqrt((dl * dl - (double)m1 * m1) * (dl * dl - (double)m2 * m2)) * t5;
+            cc = (double)m1 * m2 / (dl * (dl + 1));
+        }
+        double nxt = bb * (cb - cc) * cur - a * prev;
+        prev = cur;
+        cur = nxt;
+        o64[l + 1] = cur;
+        if (o32) o32[l + 1] = (float)cur;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Inverse SO(3) transform, one block per (beta index k, orientation, pair):
+//   S[m1][m2] = sum_{l >= max(|m1|,|m2|)} d^l_{m1m2}(beta_k) (+-1)^l I^l_{m1m2}
+// (the inverted copy of A has I^l -> (-1)^l I^l since Y_lm(-r) = (-1)^l Y_lm(r))
+// then unnormalised backward DFTs m2 -> gamma and m1 -> alpha in shared memory
+// and the real part written to grid[grid0 + o*G^3 + a + G*(k + G*g)].
+template <typename T, typename T2>
+__global__ void __launch_bounds__(256) k_isoft(const PairDev *pairs, const T2 *coef,
+                                               const T *const *dtab, T *grid) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int k = blockIdx.x, o = blockIdx.y, p = blockIdx.z;
+    const PairDev P = pairs[p];
+    const int G = P.G, L = P.L, bw = L + 1, Wc = 2 * L + 1;
+    if (k >= G || o >= P.norient) return;
+    T2 *bufA = (T2 *)smem_raw, *bufB = bufA + G * G, *tw = bufB + G * G;
+    for (int t = threadIdx.x; t < G; t += blockDim.x) {
+        double sn, cs;
+        sincospi(2.0 * t / G, &sn, &cs);
+        tw[t] = mk2<T2>(cs, sn);
+    }
+    for (int t = threadIdx.x; t < G * G; t += blockDim.x) bufA[t] = mk2<T2>(0, 0);
+    __syncthreads();
+    const T *d = dtab[bw];
+    const T2 *I = coef + P.coef0;
+    for (int t = threadIdx.x; t < Wc * Wc; t += blockDim.x) {
+        const int i1 = t / Wc, i2 = t % Wc;
+        const int m1 = (i1 <= L) ? i1 : i1 - Wc, m2 = (i2 <= L) ? i2 : i2 - Wc;
+        const int l0 = max(abs(m1), abs(m2));
+        const T *dr = d + ((long long)(k * Wc + i1) * Wc + i2) * bw;
+        T sr = 0, si = 0;
+        for (int l = l0; l <= L; ++l) {
+            T2 c = I[((long long)l * Wc + i1) * Wc + i2];
+            T dv = dr[l];
+            if (o == 1 && (l & 1)) dv = -dv;
+            sr += dv * c.x;
+            si += dv * c.y;
+        }
+        bufA[((m1 + G) % G) * G + (m2 + G) % G] = mk2<T2>(sr, si);
+    }
+    __syncthreads();
+    T2 *r1 = fft_lines(bufA, bufB, G, G, G, 1, +1, tw);       // m2 -> gamma
+    T2 *o1 = (r1 == bufA) ? bufB : bufA;
+    T2 *r2 = fft_lines(r1, o1, G, G, 1, G, +1, tw);           // m1 -> alpha
+    T *out = grid + P.grid0 + (long long)o * G * G * G + (long long)G * k;
+    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+        const int a = t % G, g = t / G;
+        out[a + (long long)G * G * g] = r2[a * G + g].x;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+void launch_sph_center(const SphBuffers &b, cudaStream_t s) {
+    k_sph_center<<<b.npairs, 256, 0, s>>>(const_cast<PairDev *>(b.pairs), b.slot2orig, b.pos1,
+                                          b.pos2, b.xa, b.xb);
+}
+
+void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s) {
+    int nth = 2 * b.nslots, bs = 128;
+    if (fp32)
+        k_sph_ylm<float2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra,
+                                                            b.rb, (float2 *)b.ylmA, (float2 *)b.ylmB,
+                                                            b.nslots);
+    else
+        k_sph_ylm<double2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra,
+                                                             b.rb, (double2 *)b.ylmA,
+                                                             (double2 *)b.ylmB, b.nslots);
+}
+
+void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s) {
+    long long nn = (long long)b.maxgroup * b.maxgroup;
+    dim3 grid((unsigned)((nn + 255) / 256), (unsigned)b.ngroups);
+    if (fp32)
+        k_sph_radial<float><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (float *)b.W, cutoff);
+    else
+        k_sph_radial<double><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (double *)b.W, cutoff);
+}
+
+void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s) {
+    dim3 grid(b.maxL + 1, b.npairs);
+    if (fp32) {
+        size_t sm = sizeof(float2) * (kMaxWM * kTB + kMaxWM * kTA + kTA * kMaxWM) + sizeof(float) * kTB * kTA;
+        cudaFuncSetAttribute(k_sph_coeff<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_sph_coeff<float, float2><<<grid, 256, sm, s>>>(b.pairs, b.groups, (const float2 *)b.ylmA,
+                                                        (const float2 *)b.ylmB, (const float *)b.W,
+                                                        (float2 *)b.coef);
+    } else {
+        size_t sm = sizeof(double2) * (kMaxWM * kTB + kMaxWM * kTA + kTA * kMaxWM) + sizeof(double) * kTB * kTA;
+        cudaFuncSetAttribute(k_sph_coeff<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_sph_coeff<double, double2><<<grid, 256, sm, s>>>(b.pairs, b.groups, (const double2 *)b.ylmA,
+                                                          (const double2 *)b.ylmB, (const double *)b.W,
+                                                          (double2 *)b.coef);
+    }
+}
+
+void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s) {
+    dim3 grid(b.maxG, 2, b.npairs);
+    if (fp32) {
+        size_t sm = sizeof(float2) * (2 * b.maxG * b.maxG + b.maxG);
+        cudaFuncSetAttribute(k_isoft<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_isoft<float, float2><<<grid, 256, sm, s>>>(b.pairs, (const float2 *)b.coef,
+                                                    (const float *const *)b.dtab, (float *)b.grid);
+    } else {
+        size_t sm = sizeof(double2) * (2 * b.maxG * b.maxG + b.maxG);
+        cudaFuncSetAttribute(k_isoft<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_isoft<double, double2><<<grid, 256, sm, s>>>(b.pairs, (const double2 *)b.coef,
+                                                      (const double *const *)b.dtab, (double *)b.grid);
+    }
+}
+
+void launch_wigner_table(int bw, double *d64, float *d32, cudaStream_t s) {
+    int W = 2 * bw - 1, n = 2 * bw * W * W;
+    k_wigner_table<<<(n + 127) / 128, 128, 0, s>>>(bw, d64, d32);
+}
+
+}  // namespace fo

@@ -1,0 +1,189 @@
+/*
+ * fastoverlap_gb300.h -- C ABI of the GB300 (sm_103a) FASTOVERLAP alignment
+ * library (libfastoverlap_gb300.so).
+ *
+ * Plain C types only: host pointers, sizes, POD structs.  Every call returns
+ * an fo_status and never exits the process.  All coordinates are flat
+ * (x, y, z) per atom in float64.  Permutation groups ("species") are given as
+ * a concatenated list of atom indices plus the size of each group, as the
+ * upstream Fortran takes them (fastoverlaputils.setperm); the index base is a
+ * parameter so Fortran callers can pass their 1-based PERMGROUP unchanged.
+ *
+ * Upstream interfaces replaced (paths inside matthewghgriffiths/fastoverlap):
+ *   fo_setperm             <- SETPERM            fastoverlap/f90/fastutils.f90:117-167
+ *   fo_cluster_align       <- CLUSTERFASTOVERLAP::ALIGN  fastoverlap/f90/fastclusters.f90:129-269
+ *                             (f2py clusterfastoverlap.align, sphericalAlignment.py:531-532)
+ *   fo_bulk_align          <- BULKFASTOVERLAP::ALIGN      fastoverlap/f90/fastbulk.f90:279-334
+ *                             and ALIGN1 (:414-499) when nwave/nfspace are given
+ *                             (f2py bulkfastoverlap.align, periodicAlignment.py:562-565)
+ *   fo_bulk_calcdefaults   <- BULKFASTOVERLAP::CALCDEFAULTS fastoverlap/f90/fastbulk.f90:253-277
+ *   fo_cluster_align_batch <- SphericalAlign.__call__ / SphericalAlignFortran.__call__
+ *                             applied to many pairs (sphericalAlignment.py:237-247,491-533)
+ *   fo_bulk_align_batch    <- PeriodicAlignFortran.align applied to many pairs
+ *                             (periodicAlignment.py:526-568)
+ *   flags in fo_cluster_pair/fo_bulk_pair replace the COMMONS globals
+ *   PERMINVOPT / OHCELLT (fastoverlap/f90/commons.f90:375-380)
+ */
+#ifndef FASTOVERLAP_GB300_H
+#define FASTOVERLAP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FO_OK = 0,
+    FO_ERR_BAD_ARGS = 1,      /* invalid sizes, groups, widths ...           */
+    FO_ERR_NO_PEAKS = 2,      /* peak search found nothing (upstream: STOP)  */
+    FO_ERR_LAP_FAILED = 3,    /* assignment failed for some atoms            */
+    FO_ERR_TIMEOUT = 4,       /* a bounded device wait gave up               */
+    FO_ERR_OOM_BUDGET = 5,    /* request does not fit the HBM budget         */
+    FO_ERR_CUDA = 6,          /* CUDA runtime error (see fo_last_error)      */
+    FO_ERR_UNIMPLEMENTED = 7,
+    FO_ERR_QUEUE_FULL = 8,    /* serving queue full                          */
+    FO_ERR_NOT_READY = 9      /* serving request still in flight             */
+} fo_status;
+
+typedef enum {
+    FO_PREC_FP64 = 0,   /* plain form: every stage in FP64                     */
+    FO_PREC_MIXED = 1   /* coefficients, SO(3)/translation grids and peak fits
+                           in FP32; Wigner-d generation, Kabsch and distances
+                           in FP64; assignment integer                         */
+} fo_precision;
+
+typedef struct fo_ctx fo_ctx;
+
+typedef struct {
+    int    device;            /* CUDA device ordinal                          */
+    int    precision;         /* fo_precision                                 */
+    size_t hbm_budget_bytes;  /* admission budget for batches / serving; 0 = 80% of free */
+    int    cutoff;            /* 1: skip atom pairs with |r_a - r_b| >= 4 sigma
+                                 (fastclusters.f90:901); 0: full pair sum as in
+                                 sphericalAlignment.py:260-273                 */
+    int    profile;           /* 1: record per-kernel CUDA-event times        */
+} fo_opts;
+
+/* per-pair description for the spherical (cluster) batch */
+typedef struct {
+    int     natoms;      /* atoms in each structure                           */
+    int     ngroups;     /* permutation groups                                */
+    int     jmax;        /* L: SO(3) bandwidth L+1, grid 2(L+1) per axis      */
+    int     nrot;        /* candidate rotations per orientation (peaks)       */
+    int     invert;      /* 1: also align the inverted copy (PERMINVOPT)      */
+    int     reserved;
+    double  sigma;       /* Gaussian width; <= 0 picks CHOOSE_KWIDTH's value  */
+    int64_t coord_off;   /* first atom of this pair in the packed coordinates */
+    int64_t perm_off;    /* first entry in the packed permutation list        */
+    int64_t group_off;   /* first entry in the packed group-size list         */
+} fo_cluster_pair;
+
+/* per-pair description for the periodic (bulk) batch */
+typedef struct {
+    int     natoms;
+    int     ngroups;
+    int     nwave;       /* K: (2K+1)^3 wave vectors; <= 0 -> ceil(1.3 N^1/3) */
+    int     nfspace;     /* M: M^3 translation grid; <= 0 -> FASTLEN(4K+3)    */
+    int     ndisps;      /* candidate displacements; <= 0 -> 10               */
+    int     reserved;
+    double  sigma;       /* <= 0 -> (V/N)^(1/3)/3                             */
+    double  box[3];      /* orthorhombic box lengths                          */
+    int64_t coord_off;
+    int64_t perm_off;
+    int64_t group_off;
+} fo_bulk_pair;
+
+/* per-pair result of either batch */
+typedef struct {
+    double dist;         /* aligned Euclidean distance (RMSD * sqrt(N))       */
+    double rmat[9];      /* row-major R: aligned = R * (+/-)centred pos2      */
+    double disp[3];      /* bulk: aligned = pos2[perm] + disp                 */
+    double overlap_max;  /* maximum of the winning overlap grid               */
+    double sigma;        /* width used                                        */
+    int    inverted;     /* 1 if -pos2 aligned best                           */
+    int    ncand;        /* candidates refined                                */
+    int    status;       /* fo_status of this pair                            */
+    int    niter;        /* assignment/rotation iterations of the winner      */
+} fo_pair_result;
+
+/* ---- context ---- */
+fo_status   fo_ctx_create(const fo_opts *opts, fo_ctx **out);
+void        fo_ctx_destroy(fo_ctx *ctx);
+const char *fo_status_string(fo_status s);
+const char *fo_last_error(const fo_ctx *ctx);
+fo_status   fo_set_precision(fo_ctx *ctx, int precision);
+
+/* ---- batched entry points (host buffers in, host buffers out) ----
+ * pos1 = target structures (COORDSB), pos2 = structures moved onto them
+ * (COORDSA); both packed as pairs[i].coord_off.. (+natoms) atoms.
+ * perm: concatenated permutation groups, `index_base` 0 or 1.
+ * aligned (optional, may be NULL): 3*sum(natoms) doubles, the aligned copy of
+ *   pos2 in pos1's centred frame (cluster) or pos1's frame (bulk), in pos1's
+ *   atom order: aligned atom j is matched with pos1 atom j.
+ * permbest (optional): sum(natoms) ints, pos2 atom matched with pos1 atom j
+ *   (same index base as perm).                                                */
+fo_status fo_cluster_align_batch(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
+                                 const double *pos1, const double *pos2,
+                                 const int *perm, const int *group_sizes, int index_base,
+                                 double *aligned, int *permbest, fo_pair_result *results);
+
+fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs,
+                              const double *pos1, const double *pos2,
+                              const int *perm, const int *group_sizes, int index_base,
+                              double *aligned, int *permbest, fo_pair_result *results);
+
+/* ---- resident plans: upload once, run many times (inputs stay in HBM) ----
+ * fo_plan_run launches the whole pipeline on the context's stream and
+ * returns without synchronising; fo_plan_wait blocks until it is done.      */
+typedef struct fo_plan fo_plan;
+fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
+                                 const double *pos1, const double *pos2,
+                                 const int *perm, const int *group_sizes, int index_base,
+                                 fo_plan **out);
+fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs,
+                              const double *pos1, const double *pos2,
+                              const int *perm, const int *group_sizes, int index_base,
+                              fo_plan **out);
+fo_status fo_plan_run(fo_plan *plan);
+fo_status fo_plan_wait(fo_plan *plan);
+fo_status fo_plan_results(fo_plan *plan, double *aligned, int *permbest,
+                          fo_pair_result *results);
+size_t    fo_plan_device_bytes(const fo_plan *plan);
+void      fo_plan_destroy(fo_plan *plan);
+
+/* ---- Fortran-compatible single-pair entry points ----
+ * fo_setperm keeps the permutation groups in the context, as SETPERM keeps
+ * them in module storage; permgroup is 1-based like the Fortran array.      */
+fo_status fo_setperm(fo_ctx *ctx, int natoms, const int *permgroup, const int *npermsize,
+                     int npermgroup);
+fo_status fo_get_bestperm(const fo_ctx *ctx, int *bestperm /* natoms, 1-based */);
+
+/* CLUSTERFASTOVERLAP::ALIGN: coordsb is centred in place, coordsa becomes the
+ * aligned, permuted copy; kwidth <= 0 is replaced by the chosen width;
+ * rmatbest is column-major 3x3 as in Fortran.  perminvopt = PERMINVOPT.     */
+fo_status fo_cluster_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms,
+                           int debug, int l, double *kwidth, int nrotations, int perminvopt,
+                           double *distance, double *dist2, double *rmatbest);
+
+/* BULKFASTOVERLAP::ALIGN (nwave = nfspace = 0) or ALIGN1 (both given). */
+fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms,
+                        int debug, double boxlx, double boxly, double boxlz,
+                        double kwidth, int ndisplacements, int nwave, int nfspace,
+                        double *distance, double *dist2);
+
+/* BULKFASTOVERLAP::CALCDEFAULTS */
+fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz,
+                               double *kernelwidth, int *nwave, int *nfspace);
+
+/* ---- profiling: per-kernel CUDA-event time of the last fo_plan_run ----
+ * names[i] receives a static string; returns the number of kernels.         */
+int fo_profile_kernels(const fo_ctx *ctx, const char **names, double *ms_total,
+                       int *launches, int cap);
+void fo_profile_reset(fo_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

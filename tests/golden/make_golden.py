@@ -1,0 +1,105 @@
+"""Generate the golden fixtures in this directory from the upstream Python code.
+
+Run in a container that has the upstream checkout (FO_REF_ROOT, read-only);
+the GPU test machine only reads the .npz files this writes.
+
+  python tests/golden/make_golden.py
+
+Fixtures:
+  lj38.npz    the upstream example pair examples/LJ38/{coords,finish} and the
+              SphericalAlign distances at Jmax 7 and 14 (published: 1.4767,
+              fastoverlap/sphericalAlignment.py:692)
+  blj256.npz  examples/BLJ256/{coords,finish}, box 5.975206329, 204:52, and
+              the PeriodicAlign distance (published 1.559,
+              fastoverlap/periodicAlignment.py:609).  The upstream periodic
+              cost matrix is transposed relative to what
+              find_best_permutation expects (periodicAlignment.py:100 vs
+              utils.py:161-165); the fixture uses a subclass that transposes
+              it, which reproduces the published value.
+  stages.npz  stage vectors from the upstream functions on seeded inputs:
+              SO(3) coefficients (calcSO3Coeffs), Wigner-d tables (SOFT.Ds),
+              inverse SOFT grid (SOFT.iSOFT), periodic overlap grid
+              (PeriodicAlign.setPos fabs), Kearsley rotation (findrotation),
+              linear assignment (the scipy solver behind the munkres shim).
+  e2e.npz     SphericalAlign / PeriodicAlign distances on seeded synthetic
+              pairs of the 38-atom and 256-atom configurations.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+
+import ref_shim  # noqa: E402
+from fastoverlap_gb300 import synth  # noqa: E402
+
+
+def main():
+    root = os.environ.get("FO_REF_ROOT", "/root/reference")
+    R = ref_shim.import_reference(root)
+    ex = os.path.join(root, "examples")
+
+    p1 = np.loadtxt(os.path.join(ex, "LJ38", "coords"))
+    p2 = np.loadtxt(os.path.join(ex, "LJ38", "finish"))
+    d14 = float(np.real(R.sph.SphericalAlign(0.3, 14)(p1, p2)[0]))
+    d7 = float(np.real(R.sph.SphericalAlign(0.3, 7)(p1, p2)[0]))
+    d7i = float(np.real(R.sph.SphericalAlign(0.3, 7)(p1, -p2)[0]))
+    np.savez(os.path.join(HERE, "lj38.npz"), pos1=p1, pos2=p2, dist_j14=d14, dist_j7=d7,
+             dist_j7_inverted=d7i, published=1.4767)
+
+    q1 = np.loadtxt(os.path.join(ex, "BLJ256", "coords"))
+    q2 = np.loadtxt(os.path.join(ex, "BLJ256", "finish"))
+    box = np.ones(3) * 5.975206329
+    pl = [np.arange(204), np.arange(204, 256)]
+
+    class Fixed(R.per.PeriodicAlign):
+        def cost_matrix(self, X1, X2):
+            return R.per.PeriodicAlign.cost_matrix(self, X1, X2).T
+
+    dper = float(Fixed(256, box, pl)(q1, q2)[0])
+    dper7 = float(Fixed(256, box, pl, scale=0.2, n=7)(q1, q2, npeaks=10)[0])
+    np.savez(os.path.join(HERE, "blj256.npz"), pos1=q1, pos2=q2, box=box, ntypeA=204, dist=dper,
+             dist_s02_n7=dper7, published=1.559)
+
+    rng = np.random.default_rng(20170212)
+    A = rng.normal(size=(20, 3)) * 1.5
+    A -= A.mean(0)
+    B = A @ synth.haar_rotation(rng).T + rng.normal(size=A.shape) * 0.05
+    B -= B.mean(0)
+    sa = R.sph.SphericalAlign(0.4, 7)
+    coeffs = sa.calcSO3Coeffs(A, B)               # [l, m1, m2], pos1 = A
+    grid = sa.soft.iSOFT(coeffs).real             # [alpha, beta, gamma]
+    ds4 = R.soft.SOFT(4).Ds
+    dkab, Rkab = R.utils.findrotation(A, B)
+    cost = rng.integers(0, 10 ** 7, size=(40, 40))
+    from scipy.optimize import linear_sum_assignment
+    _, lsa = linear_sum_assignment(cost)
+    bq1 = synth.periodic_pair(77, n=64, sizes=(48, 16))
+    pa = Fixed(64, bq1["box"], bq1["perm"], scale=0.3, n=3)
+    pa.setPos(bq1["pos1"], bq1["pos2"])
+    np.savez(os.path.join(HERE, "stages.npz"), A=A, B=B, sigma=0.4, L=7, coeffs=coeffs,
+             grid=grid, wigner_bw4=ds4, kabsch_dist=float(np.real(dkab)), kabsch_R=Rkab,
+             lap_cost=cost, lap_cols=lsa, per_pos1=bq1["pos1"], per_pos2=bq1["pos2"],
+             per_box=bq1["box"], per_sizes=np.array([48, 16]), per_sigma=0.3, per_n=3,
+             per_fabs=pa.fabs)
+
+    sph_d, sph_inv = [], []
+    for k in range(8):
+        p = synth.config0(seed_offset=k)
+        sph_d.append(float(np.real(R.sph.SphericalAlign(0.3, 7)(p["pos1"], p["pos2"])[0])))
+        sph_inv.append(p["inverted"])
+    per_d = []
+    for k in range(2):
+        p = synth.config1(seed_offset=k)
+        per_d.append(float(Fixed(256, p["box"], p["perm"], scale=0.2, n=7)(p["pos1"], p["pos2"], npeaks=10)[0]))
+    np.savez(os.path.join(HERE, "e2e.npz"), c0_seed_offsets=np.arange(8), c0_dist=np.array(sph_d),
+             c0_inverted=np.array(sph_inv), c1_seed_offsets=np.arange(2), c1_dist=np.array(per_d))
+    print("LJ38", d7, d14, d7i, "BLJ256", dper, dper7)
+    print("c0", np.round(sph_d, 6), "c1", np.round(per_d, 6))
+
+
+if __name__ == "__main__":
+    main()
