@@ -1,0 +1,373 @@
+"""Benchmark: aligned pairs/s on the 4096-pair batched spherical workload.
+
+Workload (default): 4096 cluster pairs, N ~ U{13..147} atoms, 1-3 species,
+Jmax ~ {7, 11, 15}, sigma 0.3, 10 peaks per orientation, inversion tested
+(seeded synthetic data; see fastoverlap_gb300/synth.py).  One step = one
+pass of the whole alignment pipeline over the batch.
+
+  value : batched pairs/s with inputs resident in HBM (resident plan), the
+          precision given by --precision (default mixed), device time from
+          CUDA events on the library's stream, L2 flushed between steps.
+  e2e   : the same batch through fo_cluster_align_batch with host buffers
+          (upload, pipeline, download), wall time.
+  config: also reports the plain FP64 GPU form (batched and one pair per
+          call), and the error of the mixed form against FP64.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--npairs P] [--precision mixed|fp64]
+
+For N > 1 (torchrun), every rank runs its own batch (weak scaling), timed
+between barriers; rank 0 prints max-over-ranks timing.  --impl reference
+times the CPU restatement of the reference algorithm (oracle/) on the host
+cores over a bounded sample of the same workload.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "aligned pairs/s (batched+mixed vs plain FP64 GPU, RMSD-matched); p50/p99 ms"
+WORKLOAD = ("c2: 4096 batched spherical pairs, N~U{13..147}, 1-3 species, Jmax~{7,11,15}, "
+            "sigma 0.3, 10 peaks/orientation, inversion")
+
+
+def _gen_chunk(args):
+    lo, hi = args
+    from fastoverlap_gb300 import synth
+    out = []
+    for k in range(lo, hi):
+        p = synth.config2(1, seed_offset=k)[0]
+        out.append((p["pos1"], p["pos2"], [np.asarray(g) for g in p["perm"]], p["Jmax"]))
+    return out
+
+
+def make_workload(npairs, seed_offset=0):
+    cache = "/tmp/fo_bench_c2_%d_%d.npz" % (npairs, seed_offset)
+    if os.path.exists(cache):
+        z = np.load(cache, allow_pickle=True)
+        return list(z["pairs"])
+    nproc = min(16, os.cpu_count() or 1)
+    chunks = [(seed_offset + i, seed_offset + min(i + 64, npairs)) for i in range(0, npairs, 64)]
+    ctxm = mp.get_context("spawn")
+    with ctxm.Pool(nproc) as pool:
+        parts = pool.map(_gen_chunk, chunks)
+    pairs = [x for part in parts for x in part]
+    try:
+        np.savez(cache, pairs=np.array(pairs, dtype=object))
+    except Exception:
+        pass
+    return pairs
+
+
+class ClockSampler(object):
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_run(pairs, nthreads, budget_s=20.0):
+    """Oracle (CPU restatement of the reference algorithm) on a bounded sample."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as O
+    sample = [dict(pos1=p[0], pos2=p[1], perm=p[2], Jmax=p[3], sigma=0.3) for p in pairs]
+    n = min(len(sample), max(nthreads, 8))
+    t0 = time.time()
+    O.cluster_align_many(sample[:n], nrot=10, invert=True, cutoff=True, nthreads=nthreads)
+    dt = time.time() - t0
+    done = n
+    while dt < budget_s * 0.5 and done + n <= len(sample):
+        t1 = time.time()
+        O.cluster_align_many(sample[done:done + n], nrot=10, invert=True, cutoff=True,
+                             nthreads=nthreads)
+        dt += time.time() - t1
+        done += n
+    return done / dt, done, dt
+
+
+def run_reference(args, pairs):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as O
+    O.build()
+    sample = [dict(pos1=p[0], pos2=p[1], perm=p[2], Jmax=p[3], sigma=0.3) for p in pairs]
+    per_step = max(nthreads * 2, 16)
+    for w in range(args.warmup):
+        O.cluster_align_many(sample[:nthreads], nthreads=nthreads)
+    times = []
+    done = 0
+    for s in range(args.steps):
+        chunk = [sample[(done + i) % len(sample)] for i in range(per_step)]
+        t0 = time.time()
+        O.cluster_align_many(chunk, nthreads=nthreads)
+        times.append(time.time() - t0)
+        done += per_step
+    tot = sum(times)
+    val = per_step * args.steps / tot
+    line = {"metric": METRIC, "value": val, "unit": "pairs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample_pairs_per_step": per_step,
+                       "note": "CPU restatement of the reference Fortran cluster path (oracle/), "
+                               "all host threads; the Fortran modules need gfortran/FFTW/LAPACK, "
+                               "absent on this machine"},
+            "cpu_baseline": {"value": val, "unit": "pairs/s", "cores": nthreads, "kind": "port",
+                             "sample": "%d pairs per step of the same workload" % per_step},
+            "e2e": {"value": val, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--npairs", type=int, default=4096)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-sample", type=int, default=32)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    ws, rank, local = dist_env()
+    pairs = make_workload(args.npairs, seed_offset=rank * 1000003)
+    if args.impl == "reference":
+        run_reference(args, pairs)
+        return
+    dist = init_dist(ws)
+
+    import fastoverlap_gb300 as F
+    from fastoverlap_gb300.batch import ClusterBatch
+
+    ctx = F.Context(device=local, precision=args.precision, profile=True)
+    pos1 = [p[0] for p in pairs]
+    pos2 = [p[1] for p in pairs]
+    perms = [p[2] for p in pairs]
+    jm = [p[3] for p in pairs]
+    batch = ClusterBatch(ctx, pos1, pos2, perms, Jmax=jm, scale=0.3, nrot=10, invert=True).plan()
+
+    for _ in range(args.warmup):
+        batch.plan_run()
+        batch.plan_wait()
+    ctx.profile_reset()
+    clocks = ClockSampler(local)
+    barrier(dist)
+    ctx.synchronize()
+    clocks.start()
+    step_ms = []
+    for s in range(args.steps):
+        ctx.flush_l2(512 << 20)
+        ctx.record(0)
+        batch.plan_run()
+        ctx.record(1)
+        batch.plan_wait()
+        step_ms.append(ctx.elapsed_ms(0, 1))
+    ctx.synchronize()
+    barrier(dist)
+    clk = clocks.stop()
+    prof = ctx.profile()
+    res = batch.plan_results(with_coords=True)
+    tot_ms = allmax(dist, sum(step_ms))
+    value = args.npairs * ws * args.steps / (tot_ms / 1000.0)
+
+    # end to end through the public batch API with host buffers
+    e2e_times = []
+    eb = ClusterBatch(ctx, pos1, pos2, perms, Jmax=jm, scale=0.3, nrot=10, invert=True)
+    for s in range(max(2, min(args.steps, 3))):
+        barrier(dist)
+        t0 = time.time()
+        eb.run()
+        e2e_times.append(time.time() - t0)
+    e2e_s = allmax(dist, statistics.median(e2e_times))
+    h2d = eb.pk.h2d_bytes + len(eb.desc)
+    d2h = res["result"].nbytes + 3 * 8 * eb.pk.natoms_total + 4 * eb.pk.natoms_total
+
+    if rank != 0:
+        barrier(dist)
+        return
+
+    # plain FP64 forms and accuracy of the mixed form
+    cfg_extra = {}
+    ctx64 = F.Context(device=local, precision="fp64", profile=False)
+    b64 = ClusterBatch(ctx64, pos1, pos2, perms, Jmax=jm, scale=0.3, nrot=10, invert=True).plan()
+    b64.plan_run()
+    b64.plan_wait()
+    t0 = time.time()
+    b64.plan_run()
+    b64.plan_wait()
+    t64 = time.time() - t0
+    r64 = b64.plan_results(with_coords=True)
+    cfg_extra["fp64_batched_pairs_per_s"] = args.npairs / t64
+    ns = min(args.plain_sample, args.npairs)
+    tp = time.time()
+    for k in range(ns):
+        ClusterBatch(ctx64, [pos1[k]], [pos2[k]], [perms[k]], Jmax=jm[k], scale=0.3, nrot=10,
+                     invert=True).run()
+    tp = time.time() - tp
+    plain = ns / tp
+    cfg_extra["plain_fp64_single_pair_pairs_per_s"] = plain
+    cfg_extra["speedup_vs_plain_fp64"] = value / plain
+    ok = (res["status"] == 0) & (r64["status"] == 0)
+    rel = np.abs(res["dist"][ok] - r64["dist"][ok]) / np.maximum(r64["dist"][ok], 1e-300)
+    same = [np.array_equal(a, b) for a, b, o in zip(res["perm"], r64["perm"], ok) if o]
+    cfg_extra["mixed_vs_fp64_max_rel_dist"] = float(rel.max()) if len(rel) else None
+    cfg_extra["mixed_vs_fp64_frac_rel_le_1e-5"] = float(np.mean(rel <= 1e-5)) if len(rel) else None
+    cfg_extra["mixed_vs_fp64_identical_perm_frac"] = float(np.mean(same)) if same else None
+    cfg_extra["pairs_failed"] = int((~ok).sum())
+    per_pair_ms = sorted(step_ms)
+    cfg_extra["step_ms_p50"] = float(np.percentile(per_pair_ms, 50))
+    cfg_extra["step_ms_p99"] = float(np.percentile(per_pair_ms, 99))
+
+    # roofline of the dominant kernel (live CUDA-event times of the timed steps)
+    peaks_file = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        pk = json.load(open(peaks_file))
+        hbm = float(pk["hbm_gbs"])
+        peak_src = "measured"
+    except Exception:
+        hbm = 6800.0
+        peak_src = "fallback"
+    kern = {k: v for k, v in prof.items() if k not in ("memset",)}
+    top = max(kern, key=lambda k: kern[k][0])
+    top_ms = kern[top][0] / max(1, kern[top][1])
+    tsz = 4 if args.precision == "mixed" else 8
+    r = res["result"]
+    G = np.array([2 * (j + 1) for j in jm], dtype=np.float64)
+    if top == "findpeaks":
+        # per orientation: one initial read of the grid, then per fitted peak a
+        # subtraction pass (read + write) and an argmax/sum pass (read)
+        byts = float(np.sum((2 + 3 * r["ncand"]) * G ** 3 * tsz))
+    elif top == "refine":
+        nsz = [np.array([len(g) for g in p]) for p in perms]
+        per_iter = np.array([float(np.sum(n * np.minimum(n, 60) * 12) + 48 * n.sum()) for n in nsz])
+        byts = float(np.sum(per_iter * np.maximum(r["niter"], 1) * r["ncand"]))
+    else:
+        byts = float(np.sum(2 * 2 * G ** 3 * tsz))
+    achieved = byts / (top_ms / 1000.0) / 1e9
+    roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": None, "peak_source": peak_src,
+            "kernel_ms_per_launch": top_ms,
+            "kernel_share": kern[top][0] / sum(v[0] for v in kern.values())}
+    launches = sum(v[1] for v in kern.values())
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            nth = os.cpu_count() or 1
+            v, done, dt = cpu_baseline_run(pairs, nth)
+            cpu = {"value": v, "unit": "pairs/s", "cores": nth, "kind": "port",
+                   "sample": "%d pairs of the same workload in %.1f s" % (done, dt)}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "pairs/s", "cores": 0, "kind": "port",
+                   "sample": "failed: %s" % e}
+
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64 (mixed)" if args.precision == "mixed" else "f64",
+            "data": "synthetic",
+            "config": dict({"workload": WORKLOAD, "npairs_per_gpu": args.npairs,
+                            "precision": args.precision, "l2": "flushed (512 MiB write) between steps",
+                            "kernel_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in kern.items()}},
+                           **cfg_extra),
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": args.npairs * ws / e2e_s, "unit": "pairs/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "clocks": clk, "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+
+
+if __name__ == "__main__":
+    main()

@@ -96,6 +96,13 @@ EXPORTS = {
     "fo_profile_kernels": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_char_p), _dp, _ip,
                                           ctypes.c_int]),
     "fo_profile_reset": (None, [_vp]),
+    "fo_cluster_overlap": (ctypes.c_int, [_vp, _vp, _dp, _dp, _ip, _ip, ctypes.c_int, _dp, _dp]),
+    "fo_bulk_overlap": (ctypes.c_int, [_vp, _vp, _dp, _dp, _ip, _ip, ctypes.c_int, _dp]),
+    "fo_ctx_record": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fo_ctx_elapsed_ms": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_float)]),
+    "fo_ctx_flush_l2": (ctypes.c_int, [_vp, ctypes.c_size_t]),
+    "fo_ctx_synchronize": (ctypes.c_int, [_vp]),
 }
 
 _LIB = None
@@ -179,6 +186,20 @@ class Context(object):
 
     def profile_reset(self):
         self.lib.fo_profile_reset(self.h)
+
+    def record(self, slot):
+        self.check(self.lib.fo_ctx_record(self.h, slot), "record")
+
+    def elapsed_ms(self, a, b):
+        ms = ctypes.c_float()
+        self.check(self.lib.fo_ctx_elapsed_ms(self.h, a, b, ctypes.byref(ms)), "elapsed")
+        return float(ms.value)
+
+    def flush_l2(self, nbytes=256 << 20):
+        self.check(self.lib.fo_ctx_flush_l2(self.h, nbytes), "flush_l2")
+
+    def synchronize(self):
+        self.check(self.lib.fo_ctx_synchronize(self.h), "synchronize")
 
 
 def _prec(p):

@@ -201,3 +201,48 @@ def align_periodic(pos1, pos2, boxes, perms=None, scale=0.0, nwave=0, nfspace=0,
     """Align many periodic pairs in one GPU pipeline; returns dict of arrays."""
     ctx = ctx or _lib.default_context(precision)
     return BulkBatch(ctx, pos1, pos2, boxes, perms, scale, nwave, nfspace, ndisps).run()
+
+
+def cluster_overlap(pos1, pos2, perm=None, Jmax=15, scale=0.3, precision="fp64", ctx=None):
+    """SO(3) coefficients [l, m1, m2] and the overlap grid [alpha, beta, gamma]
+    of one pair (the non-inverted orientation), computed on the GPU."""
+    ctx = ctx or _lib.default_context(precision)
+    b = ClusterBatch(ctx, [pos1], [pos2], [perm], Jmax=Jmax, scale=scale, nrot=1, invert=False)
+    L = int(Jmax)
+    W, G = 2 * L + 1, 2 * (L + 1)
+    coef = np.zeros(2 * (L + 1) * W * W)
+    grid = np.zeros(G ** 3)
+    st = ctx.lib.fo_cluster_overlap(ctx.h, _lib.vp(b.desc), _lib.d(b.pk.pos1), _lib.d(b.pk.pos2),
+                                    _lib.i(b.pk.perm), _lib.i(b.pk.sizes), 0, _lib.d(coef),
+                                    _lib.d(grid))
+    ctx.check(st, "cluster overlap")
+    c = (coef[0::2] + 1j * coef[1::2]).reshape(L + 1, W, W)
+    return c, grid.reshape(G, G, G).transpose(2, 1, 0)
+
+
+def bulk_overlap(pos1, pos2, box, perm=None, scale=0.0, nwave=0, nfspace=0, precision="fp64",
+                 ctx=None):
+    """Translation overlap grid |F| [x, y, z] of one periodic pair on the GPU."""
+    ctx = ctx or _lib.default_context(precision)
+    b = BulkBatch(ctx, [pos1], [pos2], box, [perm], scale=scale, nwave=nwave, nfspace=nfspace,
+                  ndisps=1)
+    n = len(np.asarray(pos1).reshape(-1, 3))
+    K = nwave if nwave else int(np.ceil(1.3 * n ** (1.0 / 3.0)))
+    M = nfspace if nfspace else _fastlen(4 * K + 3)
+    grid = np.zeros(M ** 3)
+    st = ctx.lib.fo_bulk_overlap(ctx.h, _lib.vp(b.desc), _lib.d(b.pk.pos1), _lib.d(b.pk.pos2),
+                                 _lib.i(b.pk.perm), _lib.i(b.pk.sizes), 0, _lib.d(grid))
+    ctx.check(st, "bulk overlap")
+    return grid.reshape(M, M, M).transpose(2, 1, 0)
+
+
+def _fastlen(n):
+    m = max(1, int(n))
+    while True:
+        k = m
+        for f in (2, 3, 5):
+            while k % f == 0:
+                k //= f
+        if k == 1:
+            return m
+        m += 1

@@ -59,6 +59,9 @@ struct fo_ctx {
     std::vector<int> bestperm;
     double prof_ms[kNumKernels] = {0};
     int prof_n[kNumKernels] = {0};
+    cudaEvent_t ev[64] = {};
+    void *flush_buf = nullptr;
+    size_t flush_bytes = 0;
 };
 
 struct fo_plan {
@@ -196,6 +199,15 @@ fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
     return FO_OK;
 }
 
+void widen(const void *src, double *dst, size_t n, bool fp32) {
+    if (fp32) {
+        const float *f = (const float *)src;
+        for (size_t i = 0; i < n; ++i) dst[i] = f[i];
+    } else {
+        memcpy(dst, src, n * sizeof(double));
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -247,6 +259,9 @@ void fo_ctx_destroy(fo_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->opts.device);
     cudaStreamSynchronize(ctx->stream);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    cudaFree(ctx->flush_buf);
     for (auto &kv : ctx->dtab) { cudaFree(kv.second.first); cudaFree(kv.second.second); }
     cudaFree(ctx->d_dtab64);
     cudaFree(ctx->d_dtab32);
@@ -692,6 +707,68 @@ fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
 }
 
 // ---------------------------------------------------------------------------
+// stage outputs of one pair
+
+fo_status fo_cluster_overlap(fo_ctx *ctx, const fo_cluster_pair *pair, const double *pos1,
+                             const double *pos2, const int *perm, const int *group_sizes,
+                             int index_base, double *coeffs, double *grid) {
+    if (!ctx || !pair) return FO_ERR_BAD_ARGS;
+    fo_cluster_pair q = *pair;
+    q.coord_off = q.perm_off = q.group_off = 0;
+    fo_plan *pl = nullptr;
+    fo_status s = fo_cluster_plan_create(ctx, 1, &q, pos1, pos2, perm, group_sizes, index_base, &pl);
+    if (s) return s;
+    cudaStream_t st = ctx->stream;
+    cudaMemsetAsync(pl->d_coef, 0, pl->coef_bytes, st);
+    fo::launch_sph_center(pl->sb, st);
+    fo::launch_sph_ylm(pl->sb, pl->fp32, st);
+    fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
+    fo::launch_sph_coeff(pl->sb, pl->fp32, st);
+    fo::launch_isoft(pl->sb, pl->fp32, st);
+    s = cuda_check(ctx, cudaStreamSynchronize(st), "cluster overlap");
+    const int L = q.jmax, W = 2 * L + 1, G = 2 * (L + 1);
+    const size_t ncoef = 2 * (size_t)(L + 1) * W * W, ngrid = (size_t)G * G * G;
+    const size_t tsz = pl->fp32 ? 4 : 8;
+    std::vector<unsigned char> buf(std::max(ncoef, ngrid) * tsz);
+    if (!s && coeffs) {
+        s = cuda_check(ctx, cudaMemcpy(buf.data(), pl->d_coef, ncoef * tsz, cudaMemcpyDeviceToHost), "copy");
+        if (!s) widen(buf.data(), coeffs, ncoef, pl->fp32);
+    }
+    if (!s && grid) {
+        s = cuda_check(ctx, cudaMemcpy(buf.data(), pl->sb.grid, ngrid * tsz, cudaMemcpyDeviceToHost), "copy");
+        if (!s) widen(buf.data(), grid, ngrid, pl->fp32);
+    }
+    fo_plan_destroy(pl);
+    return s;
+}
+
+fo_status fo_bulk_overlap(fo_ctx *ctx, const fo_bulk_pair *pair, const double *pos1,
+                          const double *pos2, const int *perm, const int *group_sizes,
+                          int index_base, double *grid) {
+    if (!ctx || !pair) return FO_ERR_BAD_ARGS;
+    fo_bulk_pair q = *pair;
+    q.coord_off = q.perm_off = q.group_off = 0;
+    fo_plan *pl = nullptr;
+    fo_status s = fo_bulk_plan_create(ctx, 1, &q, pos1, pos2, perm, group_sizes, index_base, &pl);
+    if (s) return s;
+    cudaStream_t st = ctx->stream;
+    cudaMemsetAsync(pl->d_fgrid, 0, pl->fgrid_bytes, st);
+    fo::launch_bulk_prep(pl->bb, st);
+    fo::launch_bulk_sf(pl->bb, pl->fp32, st);
+    fo::launch_bulk_fft(pl->bb, pl->fp32, st);
+    s = cuda_check(ctx, cudaStreamSynchronize(st), "bulk overlap");
+    const int M = pl->hp[0].G;
+    const size_t ngrid = (size_t)M * M * M, tsz = pl->fp32 ? 4 : 8;
+    std::vector<unsigned char> buf(ngrid * tsz);
+    if (!s && grid) {
+        s = cuda_check(ctx, cudaMemcpy(buf.data(), pl->bb.grid, ngrid * tsz, cudaMemcpyDeviceToHost), "copy");
+        if (!s) widen(buf.data(), grid, ngrid, pl->fp32);
+    }
+    fo_plan_destroy(pl);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
 // Fortran-style entry points
 fo_status fo_setperm(fo_ctx *ctx, int natoms, const int *permgroup, const int *npermsize, int npermgroup) {
     if (!ctx || natoms < 1 || !permgroup || !npermsize || npermgroup < 1) return FO_ERR_BAD_ARGS;
@@ -798,6 +875,45 @@ fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double bo
     *nwave = nw;
     *nfspace = fastlen(4 * nw + 3);
     return FO_OK;
+}
+
+fo_status fo_ctx_record(fo_ctx *ctx, int slot) {
+    if (!ctx || slot < 0 || slot >= 64) return FO_ERR_BAD_ARGS;
+    cudaSetDevice(ctx->opts.device);
+    if (!ctx->ev[slot]) {
+        fo_status s = cuda_check(ctx, cudaEventCreate(&ctx->ev[slot]), "cudaEventCreate");
+        if (s) return s;
+    }
+    return cuda_check(ctx, cudaEventRecord(ctx->ev[slot], ctx->stream), "cudaEventRecord");
+}
+
+fo_status fo_ctx_elapsed_ms(fo_ctx *ctx, int a, int b, float *ms) {
+    if (!ctx || !ms || a < 0 || b < 0 || a >= 64 || b >= 64 || !ctx->ev[a] || !ctx->ev[b])
+        return FO_ERR_BAD_ARGS;
+    fo_status s = cuda_check(ctx, cudaEventSynchronize(ctx->ev[b]), "cudaEventSynchronize");
+    if (s) return s;
+    return cuda_check(ctx, cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]), "cudaEventElapsedTime");
+}
+
+fo_status fo_ctx_flush_l2(fo_ctx *ctx, size_t bytes) {
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    cudaSetDevice(ctx->opts.device);
+    if (bytes > ctx->flush_bytes) {
+        cudaFree(ctx->flush_buf);
+        ctx->flush_buf = nullptr;
+        ctx->flush_bytes = 0;
+        fo_status s = cuda_check(ctx, cudaMalloc(&ctx->flush_buf, bytes), "cudaMalloc(flush)");
+        if (s) return s;
+        ctx->flush_bytes = bytes;
+    }
+    static int salt = 0;
+    return cuda_check(ctx, cudaMemsetAsync(ctx->flush_buf, (++salt) & 0xff, bytes, ctx->stream),
+                      "flush");
+}
+
+fo_status fo_ctx_synchronize(fo_ctx *ctx) {
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
 }
 
 int fo_profile_kernels(const fo_ctx *ctx, const char **names, double *ms_total, int *launches, int cap) {

@@ -153,6 +153,23 @@ fo_status fo_plan_results(fo_plan *plan, double *aligned, int *permbest,
 size_t    fo_plan_device_bytes(const fo_plan *plan);
 void      fo_plan_destroy(fo_plan *plan);
 
+/* ---- stage outputs of one pair (parity checks, diagnostics) ----
+ * fo_cluster_overlap: SO(3) coefficients (layout [l][m1 mod W][m2 mod W],
+ * W = 2L+1, complex as interleaved re/im, (L+1)W^2 complex values; the
+ * inverted copy's are (-1)^l times these) and the real overlap grid of the
+ * non-inverted orientation, G = 2(L+1), grid[a + G(b + G g)] -- CALCOVERLAP,
+ * fastoverlap/f90/fastclusters.f90:918-960, after FOURIERCOEFFS :868-916.
+ * fo_bulk_overlap: the modulus of the translation cross-correlation,
+ * M^3 values, grid[x + M(y + M z)] -- CALCFSPACE,
+ * fastoverlap/f90/fastbulk.f90:685-734 (without its k = 0 zeroing, as ALIGN1
+ * computes it at :437-454,522-523).  Either pointer may be NULL.            */
+fo_status fo_cluster_overlap(fo_ctx *ctx, const fo_cluster_pair *pair, const double *pos1,
+                             const double *pos2, const int *perm, const int *group_sizes,
+                             int index_base, double *coeffs, double *grid);
+fo_status fo_bulk_overlap(fo_ctx *ctx, const fo_bulk_pair *pair, const double *pos1,
+                          const double *pos2, const int *perm, const int *group_sizes,
+                          int index_base, double *grid);
+
 /* ---- Fortran-compatible single-pair entry points ----
  * fo_setperm keeps the permutation groups in the context, as SETPERM keeps
  * them in module storage; permgroup is 1-based like the Fortran array.      */
@@ -176,6 +193,16 @@ fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natom
 /* BULKFASTOVERLAP::CALCDEFAULTS */
 fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz,
                                double *kernelwidth, int *nwave, int *nfspace);
+
+/* ---- timing helpers on the context's stream (benchmarks) ----
+ * fo_ctx_record records CUDA event `slot` (0..63) on the context stream;
+ * fo_ctx_elapsed_ms reads the device time between two recorded slots (it
+ * synchronises on the later one); fo_ctx_flush_l2 writes `bytes` of
+ * scratch memory on the stream so the next launch starts with a cold L2.   */
+fo_status fo_ctx_record(fo_ctx *ctx, int slot);
+fo_status fo_ctx_elapsed_ms(fo_ctx *ctx, int slot_a, int slot_b, float *ms);
+fo_status fo_ctx_flush_l2(fo_ctx *ctx, size_t bytes);
+fo_status fo_ctx_synchronize(fo_ctx *ctx);
 
 /* ---- profiling: per-kernel CUDA-event time of the last fo_plan_run ----
  * names[i] receives a static string; returns the number of kernels.         */

@@ -1,0 +1,147 @@
+"""Host-side checks that need no GPU: C ABI exports and struct layouts,
+workload generators, batch packing, multi-process timing helpers."""
+import ctypes
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "fastoverlap_gb300.h")
+
+
+def _declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fo_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(fo):
+    from fastoverlap_gb300 import _lib
+    lib = _lib.load()
+    names = _declared_functions()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _lib.EXPORTS, "ctypes signature missing for " + name
+
+
+def test_struct_layouts_match_header(tmp_path, fo):
+    from fastoverlap_gb300 import _lib
+    src = tmp_path / "sz.c"
+    src.write_text('#include "fastoverlap_gb300.h"\n#include <stdio.h>\n#include <stddef.h>\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(fo_opts),'
+                   ' sizeof(fo_cluster_pair), sizeof(fo_bulk_pair), sizeof(fo_pair_result),'
+                   ' offsetof(fo_bulk_pair, box), offsetof(fo_pair_result, inverted));return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    want = [ctypes.sizeof(_lib.FoOpts), ctypes.sizeof(_lib.FoClusterPair),
+            ctypes.sizeof(_lib.FoBulkPair), ctypes.sizeof(_lib.FoPairResult),
+            _lib.FoBulkPair.box.offset, _lib.FoPairResult.inverted.offset]
+    assert got == want
+
+
+def test_context_without_gpu_fails_cleanly(fo):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is visible")
+    except ImportError:
+        pass
+    with pytest.raises(fo.FoError):
+        fo.Context()
+
+
+def test_config0_generator():
+    from fastoverlap_gb300 import synth
+    p = synth.config0()
+    A, B = p["pos1"], p["pos2"]
+    assert A.shape == (38, 3) and B.shape == (38, 3)
+    assert np.all(np.linalg.norm(A, axis=1) <= 1.9 + 1e-12)
+    d = np.sqrt(((A[:, None] - A[None]) ** 2).sum(-1)) + np.eye(38) * 10
+    assert d.min() >= 0.9
+    # B is A rotated, permuted, noised (and inverted for odd seeds)
+    s = -1.0 if p["inverted"] else 1.0
+    Bt = s * B
+    back = np.empty_like(A)
+    back[p["true_perm"]] = Bt
+    Rb = back @ p["rot"]
+    assert np.sqrt(((Rb - A) ** 2).sum(-1)).max() < 0.5
+
+
+def test_config1_generator():
+    from fastoverlap_gb300 import synth
+    p = synth.config1()
+    L = p["box"][0]
+    assert abs(L - (256 / 1.2) ** (1 / 3)) < 1e-12
+    A = p["pos1"]
+    d = A[:, None] - A[None]
+    d -= L * np.round(d / L)
+    d = np.sqrt((d ** 2).sum(-1)) + np.eye(256) * 10
+    assert d.min() >= 0.8
+    assert [len(g) for g in p["perm"]] == [204, 52]
+
+
+def test_config2_shapes():
+    from fastoverlap_gb300 import synth
+    ps = synth.config2(12)
+    for p in ps:
+        n = len(p["pos1"])
+        assert 13 <= n <= 147 and p["Jmax"] in (7, 11, 15)
+        assert 1 <= len(p["perm"]) <= 3 and sum(len(g) for g in p["perm"]) == n
+        assert min(len(g) for g in p["perm"]) >= 1
+
+
+def test_batch_packing_offsets():
+    from fastoverlap_gb300.batch import _Packed
+    rng = np.random.default_rng(0)
+    p1 = [rng.normal(size=(n, 3)) for n in (3, 5, 2)]
+    p2 = [rng.normal(size=(n, 3)) for n in (3, 5, 2)]
+    perms = [None, [np.array([0, 2, 4]), np.array([1, 3])], None]
+    pk = _Packed(p1, p2, perms)
+    assert list(pk.off) == [0, 3, 8] and pk.natoms_total == 10
+    assert list(pk.perm) == [0, 1, 2, 0, 2, 4, 1, 3, 0, 1]
+    assert list(pk.sizes) == [3, 3, 2, 2] and list(pk.group_off) == [0, 1, 3]
+    assert np.array_equal(pk.pos1[9:24], p1[1].ravel())
+
+
+def _allmax_worker(rank, ws, port, q):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(ws), LOCAL_RANK=str(rank),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, ROOT)
+    import bench
+    dist = bench.init_dist(ws)
+    bench.barrier(dist)
+    q.put((rank, bench.allmax(dist, 10.0 + rank)))
+    dist.destroy_process_group()
+
+
+def test_bench_max_over_ranks_gloo():
+    import multiprocessing as mp
+    ctxm = mp.get_context("spawn")
+    q = ctxm.Queue()
+    port = 29500 + os.getpid() % 1000
+    procs = [ctxm.Process(target=_allmax_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+    assert out == [(0, 11.0), (1, 11.0)]
+
+
+def test_clock_sampler_parses_reasons():
+    sys.path.insert(0, ROOT)
+    import bench
+    cs = bench.ClockSampler()
+    cs.proc = type("P", (), {"terminate": lambda s: None, "wait": lambda s, timeout=None: 0})()
+    cs.lines = ["0, 1980, 2070, 900.0, 0x0, Not Active, Not Active, Not Active, Active",
+                "0, 1990, 2070, 910.0, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    r = cs.stop()
+    assert r["sm_mhz"] == 1985 and r["sm_max_mhz"] == 2070 and r["reasons"] == ["sw_power_cap"]

@@ -1,0 +1,151 @@
+"""The CPU oracle against the upstream golden vectors (no GPU needed)."""
+import numpy as np
+import pytest
+from scipy.special import ive, sph_harm_y
+from scipy.optimize import linear_sum_assignment
+
+
+def test_ylm_matches_scipy(oracle_mod):
+    rng = np.random.default_rng(1)
+    for L in (0, 1, 7, 31):
+        x = rng.normal(size=3)
+        Y = oracle_mod.ylm(x, L)
+        r = np.linalg.norm(x)
+        th, ph = np.arccos(x[2] / r), np.arctan2(x[1], x[0])
+        for l in range(L + 1):
+            for m in range(-l, l + 1):
+                assert abs(Y[l, L + m] - sph_harm_y(l, m, th, ph)) < 1e-14
+
+
+def test_ylm_at_origin_is_finite(oracle_mod):
+    Y = oracle_mod.ylm(np.zeros(3), 5)
+    assert np.all(np.isfinite(Y))
+    assert abs(Y[0, 5] - 1 / np.sqrt(4 * np.pi)) < 1e-15
+
+
+@pytest.mark.parametrize("x", [1e-9, 1e-3, 0.3, 2.0, 17.0, 120.0, 255.0, 600.0])
+def test_sphi_matches_scipy(oracle_mod, x):
+    L = 31
+    ref = ive(np.arange(L + 1) + 0.5, x) * np.sqrt(np.pi / 2 / x) * np.exp(x)
+    got = oracle_mod.sphi(L, x)
+    ok = ref > 1e-290
+    assert np.max(np.abs(got[ok] - ref[ok]) / ref[ok]) < 1e-13
+
+
+def test_fastlen_is_5_smooth(oracle_mod):
+    def smooth(m):
+        for f in (2, 3, 5):
+            while m % f == 0:
+                m //= f
+        return m == 1
+    for n in range(1, 300):
+        m = oracle_mod.fastlen(n)
+        assert m >= n and smooth(m)
+        assert all(not smooth(k) for k in range(n, m))
+    # the two translation grids of the benchmark configurations
+    assert oracle_mod.fastlen(4 * 7 + 3) == 32 and oracle_mod.fastlen(4 * 5 + 3) == 24
+
+
+def test_coefficients_match_upstream(oracle_mod, golden):
+    g = golden("stages")
+    c = oracle_mod.cluster_coeffs(g["A"], g["B"], int(g["L"]), float(g["sigma"]), cutoff=False)
+    ref = g["coeffs"]
+    assert np.max(np.abs(c - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_wigner_table_matches_upstream(oracle_mod, golden):
+    g = golden("stages")
+    assert np.max(np.abs(oracle_mod.wigner_d(4) - g["wigner_bw4"])) < 1e-13
+
+
+def test_isoft_matches_upstream(oracle_mod, golden):
+    g = golden("stages")
+    grid = oracle_mod.isoft(g["coeffs"])
+    assert np.max(np.abs(grid - g["grid"])) <= 1e-12 * np.max(np.abs(g["grid"]))
+
+
+def test_kearsley_rotation_matches_upstream(oracle_mod, golden):
+    g = golden("stages")
+    d, R = oracle_mod.findrotation(g["A"], g["B"])
+    assert abs(d - float(g["kabsch_dist"])) < 1e-12
+    assert np.max(np.abs(R - g["kabsch_R"])) < 1e-12
+
+
+def test_jv_matches_upstream_assignment(oracle_mod, golden):
+    g = golden("stages")
+    rc, x = oracle_mod.jv(g["lap_cost"])
+    assert rc == 0
+    assert np.array_equal(x, g["lap_cols"])
+
+
+@pytest.mark.parametrize("n", [5, 37, 60])
+def test_jv_dense_optimal(oracle_mod, n):
+    rng = np.random.default_rng(n)
+    for _ in range(10):
+        c = rng.integers(0, 10 ** 7, size=(n, n))
+        rc, x = oracle_mod.jv(c)
+        r, col = linear_sum_assignment(c)
+        assert rc == 0 and c[np.arange(n), x].sum() == c[r, col].sum()
+
+
+def test_pairdists_keeps_60_nearest(oracle_mod):
+    rng = np.random.default_rng(3)
+    P, Q = rng.normal(size=(90, 3)), rng.normal(size=(90, 3))
+    cc, kk = oracle_mod.pairdists(P, Q)
+    full = ((P[:, None] - Q[None]) ** 2).sum(-1)
+    for i in range(90):
+        assert set(kk[i]) == set(np.argsort(full[i])[:60])
+        assert np.allclose(cc[i], full[i, kk[i]], rtol=0, atol=1e-12)
+        assert cc[i][0] == cc[i].max()   # heap root holds the largest kept distance
+
+
+def test_periodic_grid_matches_upstream(oracle_mod, golden):
+    g = golden("stages")
+    s = g["per_sizes"]
+    perm = [np.arange(s[0]), np.arange(s[0], s[0] + s[1])]
+    fs = oracle_mod.bulk_fspace(g["per_pos1"], g["per_pos2"], g["per_box"], perm=perm,
+                                sigma=float(g["per_sigma"]), nwave=int(g["per_n"]))
+    ref = g["per_fabs"]
+    assert fs.shape == ref.shape
+    assert np.max(np.abs(fs - ref)) <= 1e-12 * ref.max()
+
+
+def test_lj38_known_answer(oracle_mod, golden):
+    g = golden("lj38")
+    for L, ref in ((7, float(g["dist_j7"])), (14, float(g["dist_j14"]))):
+        r = oracle_mod.cluster_align(g["pos1"], g["pos2"], Jmax=L, sigma=0.3, nrot=10)
+        assert abs(r["dist"] - ref) <= 1e-10 * ref
+        assert abs(r["dist"] - float(g["published"])) < 1e-4  # published to 4 decimals
+    r = oracle_mod.cluster_align(g["pos1"], -g["pos2"], Jmax=7, sigma=0.3, nrot=10)
+    assert abs(r["dist"] - float(g["dist_j7_inverted"])) <= 1e-10 * r["dist"]
+
+
+def test_blj256_known_answer(oracle_mod, golden):
+    g = golden("blj256")
+    n = int(g["ntypeA"])
+    perm = [np.arange(n), np.arange(n, 256)]
+    r = oracle_mod.bulk_align(g["pos1"], g["pos2"], g["box"], perm=perm)
+    assert abs(r["dist"] - float(g["dist"])) <= 1e-10 * r["dist"]
+    assert abs(r["dist"] - float(g["published"])) < 5e-4
+
+
+def test_synthetic_pairs_match_upstream_python(oracle_mod, golden):
+    from fastoverlap_gb300 import synth
+    g = golden("e2e")
+    for k, ref in zip(g["c0_seed_offsets"], g["c0_dist"]):
+        p = synth.config0(int(k))
+        r = oracle_mod.cluster_align(p["pos1"], p["pos2"], perm=p["perm"], Jmax=7, sigma=0.3, nrot=10)
+        assert abs(r["dist"] - ref) <= 1e-8 * ref
+    for k, ref in zip(g["c1_seed_offsets"], g["c1_dist"]):
+        p = synth.config1(int(k))
+        r = oracle_mod.bulk_align(p["pos1"], p["pos2"], p["box"], perm=p["perm"], sigma=0.2,
+                                  nwave=7, ndisps=10)
+        assert abs(r["dist"] - ref) <= 1e-8 * ref
+
+
+def test_parity_check_detects_planted_error(oracle_mod, golden):
+    """A perturbed coefficient array must fail the same tolerance the tests use."""
+    g = golden("stages")
+    c = oracle_mod.cluster_coeffs(g["A"], g["B"], int(g["L"]), float(g["sigma"]), cutoff=False)
+    c[3, 1, 2] += 1e-9 * np.max(np.abs(c))
+    assert np.max(np.abs(c - g["coeffs"])) > 1e-12 * np.max(np.abs(g["coeffs"]))
