@@ -14,10 +14,7 @@
 #include <string>
 #include <vector>
 
-namespace fo {
-size_t refine_smem_bytes(int maxn);
-long long lap_bytes_host(int maxg);
-}  // namespace fo
+#include "fo_refine.cuh"
 
 namespace {
 
@@ -60,6 +57,9 @@ struct fo_ctx {
     double prof_ms[kNumKernels] = {0};
     int prof_n[kNumKernels] = {0};
     cudaEvent_t ev[64] = {};
+    static constexpr int kAux = 6;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork = nullptr, join[kAux] = {};
     void *flush_buf = nullptr;
     size_t flush_bytes = 0;
 };
@@ -83,6 +83,7 @@ struct fo_plan {
     void *d_coef = nullptr, *d_fgrid = nullptr;
     std::vector<cudaEvent_t> evs;
     std::vector<int> ev_kid;
+    std::vector<fo::RefineBucket> buckets;
 };
 
 namespace {
@@ -199,6 +200,89 @@ fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
     return FO_OK;
 }
 
+constexpr size_t kRefSmemCap = 96 * 1024;   // assignment arrays kept on chip up to this size
+
+struct RefAssign {
+    size_t smem;
+    long long lapstride;
+    int ct64;
+};
+
+// Shared-memory footprint of one refinement warp for a pair, and whether its
+// assignment arrays fit on chip.  dmax bounds every atom-atom distance the
+// refinement can meet; costs INT(d^2 1e6) below 2e9 are held in 32 bits.
+RefAssign ref_assign(int n, int maxg, bool fp32, double dmax) {
+    RefAssign r;
+    r.ct64 = (dmax * dmax * fo::kPScale >= 2.0e9) ? 1 : 0;
+    fo::RefLayout L;
+    fo::ref_layout(n, maxg, fp32, r.ct64 ? 8 : 4, L);
+    auto up = [](size_t b) {   // coarse classes keep the number of concurrent launches small
+        const size_t cls[] = {16384, 32768, 49152, 65536, 81920, 98304, 131072, 163840, 196608, 229376};
+        for (size_t c : cls)
+            if (b <= c) return c;
+        return (b + 4095) & ~(size_t)4095;
+    };
+    if (L.coord_end + L.lap_end <= kRefSmemCap) {
+        r.smem = up(L.coord_end + L.lap_end);
+        r.lapstride = 0;
+    } else {
+        r.smem = up(L.coord_end);
+        r.lapstride = (long long)((L.lap_end + 255) & ~(size_t)255);
+    }
+    return r;
+}
+
+int cand2pair_of(const fo_plan *pl, int c) {
+    // candidates of pair i are [cand0, cand0 + norient*nrot)
+    int lo = 0, hi = (int)pl->hp.size() - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) / 2;
+        if (pl->hp[mid].cand0 <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+void build_buckets(fo_plan *pl, const std::vector<RefAssign> &ra, std::vector<int> &cand_list) {
+    std::map<std::pair<int, size_t>, std::vector<int>> by;
+    for (size_t i = 0; i < pl->hp.size(); ++i) {
+        const fo::PairDev &P = pl->hp[i];
+        auto &v = by[{ra[i].ct64, ra[i].smem}];
+        for (int c = 0; c < P.norient * P.nrot; ++c) v.push_back(P.cand0 + c);
+    }
+    pl->buckets.clear();
+    cand_list.clear();
+    for (auto &kv : by) {
+        // heavier candidates first so the tail of each launch is short
+        std::stable_sort(kv.second.begin(), kv.second.end(), [&](int x, int y) {
+            return pl->hp[cand2pair_of(pl, x)].n > pl->hp[cand2pair_of(pl, y)].n;
+        });
+        fo::RefineBucket b;
+        b.offset = (int)cand_list.size();
+        b.count = (int)kv.second.size();
+        b.smem = kv.first.second;
+        b.ct64 = kv.first.first;
+        cand_list.insert(cand_list.end(), kv.second.begin(), kv.second.end());
+        pl->buckets.push_back(b);
+    }
+}
+
+double centred_radius(const double *X, int n) {
+    double c[3] = {0, 0, 0};
+    for (int j = 0; j < n; ++j)
+        for (int k = 0; k < 3; ++k) c[k] += X[3 * j + k];
+    double r2 = 0;
+    for (int j = 0; j < n; ++j) {
+        double s = 0;
+        for (int k = 0; k < 3; ++k) {
+            double t = X[3 * j + k] - c[k] / n;
+            s += t * t;
+        }
+        r2 = std::max(r2, s);
+    }
+    return std::sqrt(r2);
+}
+
 void widen(const void *src, double *dst, size_t n, bool fp32) {
     if (fp32) {
         const float *f = (const float *)src;
@@ -251,6 +335,17 @@ fo_status fo_ctx_create(const fo_opts *opts, fo_ctx **out) {
         delete c;
         return FO_ERR_CUDA;
     }
+    for (int a = 0; a < fo_ctx::kAux; ++a) {
+        if (cudaStreamCreateWithFlags(&c->aux[a], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->join[a], cudaEventDisableTiming) != cudaSuccess) {
+            delete c;
+            return FO_ERR_CUDA;
+        }
+    }
+    if (cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess) {
+        delete c;
+        return FO_ERR_CUDA;
+    }
     *out = c;
     return FO_OK;
 }
@@ -262,6 +357,11 @@ void fo_ctx_destroy(fo_ctx *ctx) {
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     cudaFree(ctx->flush_buf);
+    for (int a = 0; a < fo_ctx::kAux; ++a) {
+        if (ctx->aux[a]) cudaStreamDestroy(ctx->aux[a]);
+        if (ctx->join[a]) cudaEventDestroy(ctx->join[a]);
+    }
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
     for (auto &kv : ctx->dtab) { cudaFree(kv.second.first); cudaFree(kv.second.second); }
     cudaFree(ctx->d_dtab64);
     cudaFree(ctx->d_dtab32);
@@ -278,13 +378,15 @@ fo_status fo_set_precision(fo_ctx *ctx, int precision) {
 // ---------------------------------------------------------------------------
 static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1, const double *pos2,
                                    const std::vector<int> &slot2orig, const std::vector<int> &slot2pair,
-                                   const std::vector<int> &cand2pair, size_t ylm_n, size_t w_n,
+                                   const std::vector<int> &cand2pair, const std::vector<int> &cand_list,
+                                   size_t ylm_n, size_t w_n,
                                    size_t coef_n, size_t grid_n, size_t fgrid_n, long long lap_total) {
     const size_t T = pl->fp32 ? 4 : 8;
     const int np = pl->npairs, ns = pl->nslots, nc = pl->ncand;
     Carve cv;
     size_t o_pairs = cv.take<fo::PairDev>(np), o_groups = cv.take<fo::GroupDev>(pl->ngroups);
     size_t o_s2o = cv.take<int>(ns), o_s2p = cv.take<int>(ns), o_c2p = cv.take<int>(nc);
+    size_t o_clist = cv.take<int>(nc);
     size_t o_pos1 = cv.take<double>(3 * (size_t)ns), o_pos2 = cv.take<double>(3 * (size_t)ns);
     size_t o_xa = cv.take<double>(3 * (size_t)ns), o_xb = cv.take<double>(3 * (size_t)ns);
     size_t o_ra = cv.take<double>(ns), o_rb = cv.take<double>(ns);
@@ -314,6 +416,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     cudaMemcpyAsync(P(o_s2o), slot2orig.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(P(o_s2p), slot2pair.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(P(o_c2p), cand2pair.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(P(o_clist), cand_list.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(P(o_pos1), pos1, 3 * (size_t)ns * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(P(o_pos2), pos2, 3 * (size_t)ns * sizeof(double), cudaMemcpyHostToDevice, st);
     s = cuda_check(ctx, cudaStreamSynchronize(st), "plan upload");
@@ -385,6 +488,10 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     r.ncand = nc;
     r.maxG = pl->maxG;
     r.maxn = pl->maxn;
+    r.cand_list = (const int *)P(o_clist);
+    r.buckets = pl->buckets.data();
+    r.nbuckets = (int)pl->buckets.size();
+    r.fp32 = pl->fp32;
     pl->d_pstatus = r.pstatus;
     pl->d_npeaks = r.npeaks;
     return FO_OK;
@@ -406,6 +513,8 @@ fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair 
     std::vector<int> slot2orig, slot2pair, cand2pair;
     std::vector<double> hpos1, hpos2;
     std::vector<int> bws;
+    std::vector<RefAssign> rassign;
+    std::vector<int> cand_list;
     long long ylm_n = 0, w_n = 0, coef_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
     int atom0 = 0, cand0 = 0;
     for (int i = 0; i < npairs; ++i) {
@@ -454,9 +563,14 @@ fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair 
             pl->maxgroup = std::max(pl->maxgroup, gn);
             pl->hg.push_back(G);
         }
-        P.lapstride = fo::lap_bytes_host(maxg);
-        P.lap0 = lap_total;
-        lap_total += (long long)P.norient * P.nrot * P.lapstride;
+        {
+            double dmax = centred_radius(pos1 + 3 * q.coord_off, n) + centred_radius(pos2 + 3 * q.coord_off, n);
+            RefAssign ra = ref_assign(n, maxg, pl->fp32, dmax);
+            P.lapstride = ra.lapstride;
+            P.lap0 = lap_total;
+            lap_total += (long long)P.norient * P.nrot * P.lapstride;
+            rassign.push_back(ra);
+        }
         pl->hp.push_back(P);
         pl->caller_off.push_back(q.coord_off);
         for (int s = 0; s < n; ++s) {
@@ -484,8 +598,9 @@ fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair 
     bws.erase(std::unique(bws.begin(), bws.end()), bws.end());
     fo_status s = ensure_dtabs(ctx, bws);
     if (s) { delete pl; return s; }
+    build_buckets(pl, rassign, cand_list);
     s = plan_common_alloc(ctx, pl, hpos1.data(), hpos2.data(), slot2orig, slot2pair, cand2pair,
-                          ylm_n, w_n, coef_n, grid_n, 0, lap_total);
+                          cand_list, ylm_n, w_n, coef_n, grid_n, 0, lap_total);
     if (s) { fo_plan_destroy(pl); return s; }
     pl->sb.dtab = pl->fp32 ? (const void *const *)ctx->d_dtab32 : (const void *const *)ctx->d_dtab64;
     *out = pl;
@@ -507,6 +622,8 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
     pl->index_base = index_base;
     std::vector<int> slot2orig, slot2pair, cand2pair;
     std::vector<double> hpos1, hpos2;
+    std::vector<RefAssign> rassign;
+    std::vector<int> cand_list;
     long long fgrid_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
     int atom0 = 0, cand0 = 0;
     for (int i = 0; i < npairs; ++i) {
@@ -557,9 +674,14 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
             maxg = std::max(maxg, gn);
             pl->hg.push_back(G);
         }
-        P.lapstride = fo::lap_bytes_host(maxg);
-        P.lap0 = lap_total;
-        lap_total += (long long)P.nrot * P.lapstride;
+        {
+            double dmax = 0.5 * std::sqrt(q.box[0] * q.box[0] + q.box[1] * q.box[1] + q.box[2] * q.box[2]);
+            RefAssign ra = ref_assign(n, maxg, pl->fp32, dmax);
+            P.lapstride = ra.lapstride;
+            P.lap0 = lap_total;
+            lap_total += (long long)P.nrot * P.lapstride;
+            rassign.push_back(ra);
+        }
         pl->hp.push_back(P);
         pl->caller_off.push_back(q.coord_off);
         for (int s = 0; s < n; ++s) {
@@ -581,8 +703,9 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
     pl->nslots = atom0;
     pl->ncand = cand0;
     pl->ngroups = (int)pl->hg.size();
+    build_buckets(pl, rassign, cand_list);
     fo_status s = plan_common_alloc(ctx, pl, hpos1.data(), hpos2.data(), slot2orig, slot2pair,
-                                    cand2pair, 0, 0, 0, grid_n, fgrid_n, lap_total);
+                                    cand2pair, cand_list, 0, 0, 0, grid_n, fgrid_n, lap_total);
     if (s) { fo_plan_destroy(pl); return s; }
     *out = pl;
     return FO_OK;
@@ -615,7 +738,8 @@ fo_status fo_plan_run(fo_plan *pl) {
         fo::launch_bulk_fft(pl->bb, pl->fp32, st); rec_event(pl, K_BFFT);
     }
     fo::launch_findpeaks(pl->rb, pl->fp32, st); rec_event(pl, K_PEAKS);
-    fo::launch_refine(pl->rb, st);              rec_event(pl, K_REFINE);
+    fo::launch_refine(pl->rb, st, ctx->aux, fo_ctx::kAux, ctx->fork, ctx->join);
+    rec_event(pl, K_REFINE);
     fo::launch_select(pl->rb, st);              rec_event(pl, K_SELECT);
     return cuda_check(ctx, cudaGetLastError(), "kernel launch");
 }
@@ -900,6 +1024,11 @@ fo_status fo_ctx_flush_l2(fo_ctx *ctx, size_t bytes) {
     cudaSetDevice(ctx->opts.device);
     if (bytes > ctx->flush_bytes) {
         cudaFree(ctx->flush_buf);
+    for (int a = 0; a < fo_ctx::kAux; ++a) {
+        if (ctx->aux[a]) cudaStreamDestroy(ctx->aux[a]);
+        if (ctx->join[a]) cudaEventDestroy(ctx->join[a]);
+    }
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
         ctx->flush_buf = nullptr;
         ctx->flush_bytes = 0;
         fo_status s = cuda_check(ctx, cudaMalloc(&ctx->flush_buf, bytes), "cudaMalloc(flush)");

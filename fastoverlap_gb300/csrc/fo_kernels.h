@@ -47,6 +47,12 @@ void launch_bulk_sf(const BulkBuffers &b, bool fp32, cudaStream_t s);
 void launch_bulk_fft(const BulkBuffers &b, bool fp32, cudaStream_t s);
 
 // peaks and refinement (shared)
+struct RefineBucket {
+    int offset, count;  // slice of cand_list
+    size_t smem;        // dynamic shared memory per candidate (one warp)
+    int ct64;           // 64-bit integer costs
+};
+
 struct RefineBuffers {
     const PairDev *pairs;
     const GroupDev *groups;
@@ -66,9 +72,14 @@ struct RefineBuffers {
     double *aligned;        // 3 per atom, original order
     int *permbest;          // per atom, original order
     int npairs, ncand, maxG, maxn;
+    const int *cand_list;          // device: candidate ids grouped by bucket
+    const RefineBucket *buckets;   // host
+    int nbuckets;
+    bool fp32;
 };
 void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s);
-void launch_refine(const RefineBuffers &b, cudaStream_t s);
+void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,
+                   cudaEvent_t fork, cudaEvent_t *join);
 void launch_select(const RefineBuffers &b, cudaStream_t s);
 
 }  // namespace fo

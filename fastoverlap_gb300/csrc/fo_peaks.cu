@@ -12,6 +12,7 @@
 namespace fo {
 
 constexpr int kMaxWin = 7;  // largest window half-width handled on chip
+constexpr int kPeakThreads = 64;
 
 struct LMShared {
     double H[66];   // packed lower triangle of J^T J
@@ -99,18 +100,20 @@ __device__ int lm_fit_warp(LMShared &S, const T *win, int w, double tol) {
                         if (a == b) v += lambda * fmax(S.H[q], 1e-30);
                         S.A[q] = v;
                     }
+                double inv[11];
                 for (int j = 0; j < 11 && ok; ++j) {
                     int jj = j * (j + 1) / 2;
                     double s = S.A[jj + j];
                     for (int k = 0; k < j; ++k) s -= S.A[jj + k] * S.A[jj + k];
                     if (!(s > 0.0)) { ok = 0; break; }
                     double djj = sqrt(s);
+                    inv[j] = 1.0 / djj;
                     S.A[jj + j] = djj;
                     for (int i = j + 1; i < 11; ++i) {
                         int ii = i * (i + 1) / 2;
                         double t = S.A[ii + j];
                         for (int k = 0; k < j; ++k) t -= S.A[ii + k] * S.A[jj + k];
-                        S.A[ii + j] = t / djj;
+                        S.A[ii + j] = t * inv[j];
                     }
                 }
                 if (ok) {
@@ -119,12 +122,12 @@ __device__ int lm_fit_warp(LMShared &S, const T *win, int w, double tol) {
                         int ii = i * (i + 1) / 2;
                         double t = -S.g[i];
                         for (int k = 0; k < i; ++k) t -= S.A[ii + k] * y[k];
-                        y[i] = t / S.A[ii + i];
+                        y[i] = t * inv[i];
                     }
                     for (int i = 10; i >= 0; --i) {
                         double t = y[i];
                         for (int k = i + 1; k < 11; ++k) t -= S.A[k * (k + 1) / 2 + i] * S.dl[k];
-                        S.dl[i] = t / S.A[i * (i + 1) / 2 + i];
+                        S.dl[i] = t * inv[i];
                     }
                     for (int a = 0; a < 11; ++a) S.pn[a] = S.p[a] + S.dl[a];
                 }
@@ -198,10 +201,51 @@ __device__ void block_argmax_sum(const T *f, long long N, T &mx, long long &amax
     __syncthreads();
 }
 
+// f -= model(p, q - c) over the whole G^3 grid, then block-wide (max, first
+// index) and sum of the result; 32-bit index counters, one pass.
+template <typename T>
+__device__ void subtract_argmax_sum(T *f, int G, const double *pp, double c1, double c2, double c3,
+                                    T &mx, long long &amax, double &sum, double *sred, T *vred,
+                                    long long *ired) {
+    const int N = G * G * G, step = blockDim.x;
+    int i = threadIdx.x, i1 = i % G, i2 = (i / G) % G, i3 = i / (G * G);
+    const int d1 = step % G, d2 = (step / G) % G, d3 = step / (G * G);
+    T best = -INFINITY;
+    int bi = N;
+    double s = 0;
+    for (; i < N; i += step) {
+        T v = f[i] - peak_model<T>(pp, T(i1 + 1 - c1), T(i2 + 1 - c2), T(i3 + 1 - c3), (T *)nullptr);
+        f[i] = v;
+        s += (double)v;
+        if (v > best) { best = v; bi = i; }
+        i1 += d1; i2 += d2; i3 += d3;
+        if (i1 >= G) { i1 -= G; ++i2; }
+        if (i2 >= G) { i2 -= G; ++i3; }
+    }
+    long long bl = bi;
+    for (int o = 16; o > 0; o >>= 1) {
+        T ov = __shfl_xor_sync(0xffffffffu, best, o);
+        long long oi = __shfl_xor_sync(0xffffffffu, bl, o);
+        if (ov > best || (ov == best && oi < bl)) { best = ov; bl = oi; }
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) { vred[wid] = best; ired[wid] = bl; sred[wid] = s; }
+    __syncthreads();
+    best = vred[0]; bl = ired[0]; s = sred[0];
+    for (int w = 1; w < nw; ++w) {
+        if (vred[w] > best || (vred[w] == best && ired[w] < bl)) { best = vred[w]; bl = ired[w]; }
+        s += sred[w];
+    }
+    mx = best; amax = bl; sum = s;
+    __syncthreads();
+}
+
 // One block per (orientation, pair).  Peaks are written as 1-based
 // fractional grid coordinates (as FINDPEAKS returns them).
 template <typename T>
-__global__ void __launch_bounds__(256) k_findpeaks(const PairDev *pairs, T *grids, double *omax,
+__global__ void __launch_bounds__(kPeakThreads) k_findpeaks(const PairDev *pairs, T *grids, double *omax,
                                                    double *peaks, int *npeaks, int *pstatus,
                                                    double tol) {
     __shared__ LMShared S;
@@ -254,16 +298,12 @@ __global__ void __launch_bounds__(256) k_findpeaks(const PairDev *pairs, T *grid
                 pk[3 * nfound + 2] = c3;
             }
             ++nfound;
-            // subtract the fitted peak (not wrapped) and its mean level
+            // subtract the fitted peak (not wrapped) and its mean level; the same
+            // pass finds the next first maximum and the new grid sum
             double pp[11];
             for (int a = 0; a < 11; ++a) pp[a] = S.p[a];
             __syncthreads();
-            for (long long i = threadIdx.x; i < N; i += blockDim.x) {
-                int i1 = (int)(i % G), i2 = (int)((i / G) % G), i3 = (int)(i / ((long long)G * G));
-                f[i] -= peak_model<T>(pp, T(i1 + 1 - c1), T(i2 + 1 - c2), T(i3 + 1 - c3), (T *)nullptr);
-            }
-            __syncthreads();
-            block_argmax_sum<T>(f, N, mx, amax, sum, sred, vred, ired);
+            subtract_argmax_sum<T>(f, G, pp, c1, c2, c3, mx, amax, sum, sred, vred, ired);
         }
         if (nfound == 0) {
             ++width;
@@ -279,10 +319,10 @@ __global__ void __launch_bounds__(256) k_findpeaks(const PairDev *pairs, T *grid
 void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s) {
     dim3 grid(2, b.npairs);
     if (fp32)
-        k_findpeaks<float><<<grid, 256, 0, s>>>(b.pairs, (float *)b.grid, b.overlap_max, b.peaks,
+        k_findpeaks<float><<<grid, kPeakThreads, 0, s>>>(b.pairs, (float *)b.grid, b.overlap_max, b.peaks,
                                                b.npeaks, b.pstatus, 1e-5);
     else
-        k_findpeaks<double><<<grid, 256, 0, s>>>(b.pairs, (double *)b.grid, b.overlap_max, b.peaks,
+        k_findpeaks<double><<<grid, kPeakThreads, 0, s>>>(b.pairs, (double *)b.grid, b.overlap_max, b.peaks,
                                                 b.npeaks, b.pstatus, 1e-6);
 }
 

@@ -1,12 +1,15 @@
 // fo_refine.cu -- candidate refinement and selection.
 //
-// One block per candidate (pair, orientation, peak): rotate (cluster) or shift
+// One warp per candidate (pair, orientation, peak): rotate (cluster) or shift
 // (bulk) the moved structure by the candidate, then alternate
 //   per-group squared distances (60 nearest per row when a group has more
 //   than 60 atoms) -> integer costs INT(d^2 * 1e6) -> sparse Jonker-Volgenant
 //   assignment -> Kearsley rotation (cluster) or mean minimum-image
 //   displacement (bulk)
 // until no atom changes partner, the distance grows, or 21 tries.
+// Candidates are launched in buckets of equal shared-memory footprint so
+// small problems pack many warps per SM; the assignment arrays live in
+// shared memory when they fit and in per-candidate global scratch otherwise.
 //
 // Reference behaviour (matthewghgriffiths/fastoverlap):
 //   ITERATIVEALIGN   fastoverlap/f90/alignutils.f90:111-286
@@ -21,408 +24,555 @@
 #include "../../include/fastoverlap_gb300.h"
 #include "fo_common.cuh"
 #include "fo_kernels.h"
+#include "fo_refine.cuh"
 
 namespace fo {
 
-struct LapView {
-    long long *cc;
-    int *kk;
-    long long *v, *d;
-    int *x, *y, *lab, *fr, *todo;
-    unsigned char *ok;
-};
+constexpr unsigned kFull = 0xffffffffu;
+constexpr long long kLLMax = 0x7fffffffffffffffLL;
 
-__host__ __device__ inline long long lap_align8(long long b) { return (b + 7) & ~7LL; }
-
-__host__ __device__ inline long long lap_bytes(int maxg) {
-    int m = maxg < kMaxNei ? maxg : kMaxNei;
-    long long b = 0;
-    b += lap_align8(8LL * maxg * m);
-    b += lap_align8(4LL * maxg * m);
-    b += 2 * lap_align8(8LL * maxg);
-    b += 5 * lap_align8(4LL * maxg);
-    b += lap_align8(maxg);
-    return b;
+__device__ __forceinline__ long long wmin_ll(long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        long long w = __shfl_xor_sync(kFull, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
 }
 
-__device__ inline LapView lap_view(unsigned char *base, int maxg) {
-    int m = maxg < kMaxNei ? maxg : kMaxNei;
-    LapView L;
-    long long o = 0;
-    L.cc = (long long *)(base + o); o += lap_align8(8LL * maxg * m);
-    L.kk = (int *)(base + o); o += lap_align8(4LL * maxg * m);
-    L.v = (long long *)(base + o); o += lap_align8(8LL * maxg);
-    L.d = (long long *)(base + o); o += lap_align8(8LL * maxg);
-    L.x = (int *)(base + o); o += lap_align8(4LL * maxg);
-    L.y = (int *)(base + o); o += lap_align8(4LL * maxg);
-    L.lab = (int *)(base + o); o += lap_align8(4LL * maxg);
-    L.fr = (int *)(base + o); o += lap_align8(4LL * maxg);
-    L.todo = (int *)(base + o); o += lap_align8(4LL * maxg);
-    L.ok = base + o;
-    return L;
-}
+// ---------------------------------------------------------------------------
+// Sparse Jonker-Volgenant (Computing 38, 1987) executed by one warp.  The
+// sequence of steps -- column reduction, reduction transfer in row order,
+// two augmenting-row-reduction passes over the free list, shortest
+// augmenting paths -- and every tie rule are those of the sequential method
+// (first row wins a column minimum; the lowest scan position wins a row
+// minimum; the label list is searched last-in first-out; the first free
+// column in scan / index order ends a path).  Only the scans inside a step
+// (a row's <= 60 entries, or all columns) are spread over the 32 lanes, so
+// the assignment is the one the sequential method produces.  Rows have a
+// fixed width m; dense rows (m == n) have implicit column index t.  All
+// lanes must call; returns 0 on success, > 0 when the matching fails.
+template <typename CT>
+__device__ int jv_warp(const int n, const int m, const bool dense, const CT *__restrict__ cc,
+                       const unsigned short *__restrict__ kk, long long *v, long long *dd, int *x,
+                       int *y, int *lab, int *fr, int *todo, unsigned char *ok) {
+    const int lane = threadIdx.x & 31;
+    const unsigned ltmask = (1u << lane) - 1u;
+    auto COL = [&](int i, int t) -> int { return dense ? t : (int)kk[(long long)i * m + t]; };
+    auto CST = [&](int i, int t) -> long long { return (long long)cc[(long long)i * m + t]; };
 
-// Sparse Jonker-Volgenant (Computing 38, 1987) on CSR rows of fixed width m:
-// column reduction, reduction transfer, two augmenting-row-reduction passes,
-// shortest augmenting paths.  Sequential (one thread).  Returns 0 on success;
-// a failed matching leaves x[i] = -1 for unmatched rows.  Every loop is
-// bounded; a guard trip reports failure instead of spinning.
-__device__ int jv_sparse(int n, int m, const long long *cc, const int *kk, LapView &L) {
-    long long *v = L.v, *dd = L.d;
-    int *x = L.x, *y = L.y, *lab = L.lab, *fr = L.fr, *todo = L.todo;
-    unsigned char *ok = L.ok;  // also used as the "several minima" flag in phase 1
-    for (int j = 0; j < n; ++j) { v[j] = kBigInt; y[j] = -1; ok[j] = 0; }
+    // 1. column reduction: v_j = min_i c_ij, the first row attaining it owns j.
+    // Rows in order; a row's columns are distinct, so lanes never collide.
+    for (int j = lane; j < n; j += 32) { v[j] = kBigInt; y[j] = -1; }
+    __syncwarp();
     for (int i = 0; i < n; ++i) {
-        x[i] = -1;
-        for (int t = i * m; t < i * m + m; ++t) {
-            int j = kk[t];
-            if (cc[t] < v[j]) { v[j] = cc[t]; y[j] = i; }
+        for (int t = lane; t < m; t += 32) {
+            const int j = COL(i, t);
+            const long long c = CST(i, t);
+            if (c < v[j]) { v[j] = c; y[j] = i; }
         }
+        __syncwarp();
     }
-    for (int j = n - 1; j >= 0; --j) {
+    int bad = 0;
+    for (int j = lane; j < n; j += 32)
+        if (y[j] < 0) bad = 1;
+    if (__any_sync(kFull, bad)) return 1;
+    for (int i = lane; i < n; i += 32) { x[i] = -1; lab[i] = 0; }
+    __syncwarp();
+    // columns are visited from the last: a row keeps the highest of its columns
+    for (int j = lane; j < n; j += 32) {
         int i = y[j];
-        if (i < 0) return 1;
-        if (x[i] >= 0) { ok[i] = 1; y[j] = -1; }
-        else x[i] = j;
+        atomicMax(&x[i], j);
+        atomicAdd(&lab[i], 1);
     }
+    __syncwarp();
+    for (int j = lane; j < n; j += 32) {
+        int i = y[j];
+        if (x[i] != j) y[j] = -1;
+    }
+    for (int i = lane; i < n; i += 32) ok[i] = (lab[i] > 1);  // row owns several minima
+    __syncwarp();
+
+    // 2. reduction transfer, rows in order
     int nfree = 0;
     for (int i = 0; i < n; ++i) {
-        if (x[i] < 0) fr[nfree++] = i;
-        else if (ok[i]) ok[i] = 0;
-        else {
-            int j1 = x[i];
-            long long mn = kBigInt;
-            for (int t = i * m; t < i * m + m; ++t) {
-                int j = kk[t];
-                if (j == j1) continue;
-                if (cc[t] - v[j] < mn) mn = cc[t] - v[j];
-            }
-            v[j1] -= mn;
+        const int xi = x[i];
+        if (xi < 0) {
+            if (lane == 0) fr[nfree] = i;
+            ++nfree;
+            continue;
         }
+        if (ok[i]) continue;
+        long long mn = kBigInt;
+        for (int t = lane; t < m; t += 32) {
+            int j = COL(i, t);
+            if (j == xi) continue;
+            long long h = CST(i, t) - v[j];
+            mn = h < mn ? h : mn;
+        }
+        mn = wmin_ll(mn);
+        __syncwarp();
+        if (lane == 0) v[xi] -= mn;
+        __syncwarp();
     }
+    __syncwarp();
     if (nfree == 0) return 0;
+
+    // 3. augmenting row reduction, two passes
     long long guard = 0;
     const long long gmax = 64LL * n * (long long)n * m + 100000;
     int j0 = -1, j1 = -1;
     for (int pass = 0; pass < 2 && nfree > 0; ++pass) {
-        int l0 = nfree, k = 0;
+        const int l0 = nfree;
+        int k = 0;
         nfree = 0;
         while (k < l0) {
             if (++guard > gmax) return 9;
-            int i = fr[k++];
-            long long u1 = kBigInt, u2 = kBigInt;
-            for (int t = i * m; t < i * m + m; ++t) {
-                int j = kk[t];
-                long long h = cc[t] - v[j];
-                if (h < u2) {
-                    if (h >= u1) { u2 = h; j1 = j; }
-                    else { u2 = u1; u1 = h; j1 = j0; j0 = j; }
-                }
+            const int i = fr[k++];
+            long long h1 = kLLMax, h2 = kLLMax;
+            int t1 = 0x7fffffff, t2 = 0x7fffffff, cnt = 0;
+            for (int t = lane; t < m; t += 32) {
+                long long h = CST(i, t) - v[COL(i, t)];
+                if (!(h < kBigInt)) continue;   // never enters the two smallest
+                ++cnt;
+                if (h < h1 || (h == h1 && t < t1)) { h2 = h1; t2 = t1; h1 = h; t1 = t; }
+                else if (h < h2 || (h == h2 && t < t2)) { h2 = h; t2 = t; }
             }
+            for (int o = 16; o > 0; o >>= 1) {
+                long long oh1 = __shfl_xor_sync(kFull, h1, o), oh2 = __shfl_xor_sync(kFull, h2, o);
+                int ot1 = __shfl_xor_sync(kFull, t1, o), ot2 = __shfl_xor_sync(kFull, t2, o);
+                cnt += __shfl_xor_sync(kFull, cnt, o);
+                bool afirst = (h1 < oh1) || (h1 == oh1 && t1 < ot1);
+                long long fh, sh;
+                int ft, st;
+                if (afirst) {
+                    fh = h1; ft = t1;
+                    bool a2 = (h2 < oh1) || (h2 == oh1 && t2 < ot1);
+                    sh = a2 ? h2 : oh1; st = a2 ? t2 : ot1;
+                } else {
+                    fh = oh1; ft = ot1;
+                    bool b2 = (oh2 < h1) || (oh2 == h1 && ot2 < t1);
+                    sh = b2 ? oh2 : h1; st = b2 ? ot2 : t1;
+                }
+                h1 = fh; t1 = ft; h2 = sh; t2 = st;
+            }
+            long long u1, u2;
+            if (cnt >= 2) { u1 = h1; u2 = h2; j0 = COL(i, t1); j1 = COL(i, t2); }
+            else if (cnt == 1) { u1 = h1; u2 = kBigInt; j1 = j0; j0 = COL(i, t1); }
+            else { u1 = kBigInt; u2 = kBigInt; }
             if (j0 < 0) return 2;
             int i0 = y[j0];
-            bool reinsert = false;
+            bool reins = false;
+            __syncwarp();
             if (u1 < u2) {
-                v[j0] = v[j0] - u2 + u1;
-                reinsert = (i0 >= 0);
+                if (lane == 0) v[j0] = v[j0] - u2 + u1;
+                reins = (i0 >= 0);
             } else if (i0 >= 0) {
                 if (j1 < 0) return 3;
                 j0 = j1;
                 i0 = y[j1];
-                reinsert = (i0 >= 0);
+                reins = (i0 >= 0);
             }
-            if (reinsert) {
-                if (u1 < u2) fr[--k] = i0;
-                else fr[nfree++] = i0;
+            if (reins) {
+                if (u1 < u2) {
+                    --k;
+                    if (lane == 0) fr[k] = i0;
+                } else {
+                    if (lane == 0) fr[nfree] = i0;
+                    ++nfree;
+                }
             }
-            x[i] = j0;
-            y[j0] = i;
+            if (lane == 0) { x[i] = j0; y[j0] = i; }
+            __syncwarp();
         }
     }
+
+    // 4. shortest augmenting paths for the remaining free rows
     const int l0 = nfree;
     for (int f = 0; f < l0; ++f) {
-        for (int j = 0; j < n; ++j) { ok[j] = 0; dd[j] = kBigInt; }
-        long long mn = kBigInt;
+        for (int j = lane; j < n; j += 32) { ok[j] = 0; dd[j] = kBigInt; }
+        __syncwarp();
         const int i0 = fr[f];
         int td = n - 1, k = 0, jend = -1;
         bool price = false;
-        for (int t = i0 * m; t < i0 * m + m; ++t) {
-            int j = kk[t];
-            long long dj = cc[t] - v[j];
-            dd[j] = dj;
-            lab[j] = i0;
-            if (dj <= mn) {
-                if (dj < mn) { mn = dj; k = 0; }
-                todo[k++] = j;
+        long long hl[2];
+        int jl[2];
+        for (int q = 0; q < 2; ++q) {
+            int t = lane + 32 * q;
+            hl[q] = kLLMax;
+            jl[q] = -1;
+            if (t < m) {
+                int j = COL(i0, t);
+                long long h = CST(i0, t) - v[j];
+                dd[j] = h;
+                lab[j] = i0;
+                hl[q] = h;
+                jl[q] = j;
             }
         }
-        for (int h = 0; h < k; ++h) {
-            int j = todo[h];
-            if (y[j] < 0) { jend = j; break; }
-            ok[j] = 1;
+        long long mn = wmin_ll(hl[0] < hl[1] ? hl[0] : hl[1]);
+        if (mn > kBigInt) mn = kBigInt;
+        __syncwarp();
+        for (int q = 0; q < 2; ++q) {
+            bool sel = (hl[q] == mn);
+            unsigned msk = __ballot_sync(kFull, sel);
+            if (sel) todo[k + __popc(msk & ltmask)] = jl[q];
+            k += __popc(msk);
         }
-        while (jend < 0) {
-            if (++guard > gmax) return 9;
-            if (k == 0) return 4;
-            int jc = todo[--k];
-            int i = y[jc];
-            todo[td--] = jc;
-            int t = i * m;
-            while (t < i * m + m && kk[t] != jc) ++t;
-            if (t == i * m + m) return 5;
-            long long h = cc[t] - v[jc] - mn;
-            for (t = i * m; t < i * m + m; ++t) {
-                int j = kk[t];
-                if (ok[j]) continue;
-                long long vj = cc[t] - h - v[j];
-                if (vj < dd[j]) {
-                    dd[j] = vj;
-                    lab[j] = i;
-                    if (vj == mn) {
-                        if (y[j] < 0) { jend = j; price = true; break; }
-                        todo[k++] = j;
-                        ok[j] = 1;
-                    }
-                }
-            }
-            if (jend >= 0) break;
-            if (k != 0) continue;
-            mn = kBigInt - 1;
-            for (int j = 0; j < n; ++j) {
-                if (dd[j] <= mn && !ok[j]) {
-                    if (dd[j] < mn) { mn = dd[j]; k = 0; }
-                    todo[k++] = j;
-                }
-            }
-            for (int h2 = 0; h2 < k; ++h2) {
-                int j = todo[h2];
-                if (y[j] < 0) { jend = j; price = true; break; }
+        __syncwarp();
+        for (int b = 0; b < k && jend < 0; b += 32) {   // first free column ends the search
+            int h = b + lane, j = (h < k) ? todo[h] : -1;
+            bool fre = (h < k) && y[j] < 0;
+            unsigned fm = __ballot_sync(kFull, fre);
+            if (fm) {
+                int first = b + __ffs(fm) - 1;
+                if (h < first) ok[j] = 1;
+                jend = todo[first];
+            } else if (h < k) {
                 ok[j] = 1;
             }
         }
+        __syncwarp();
+        while (jend < 0) {
+            if (++guard > gmax) return 9;
+            if (k == 0) return 4;
+            --k;
+            const int jc = todo[k];
+            const int i = y[jc];
+            __syncwarp();
+            if (lane == 0) todo[td] = jc;
+            --td;
+            int tpos = -1;
+            for (int q = 0; q < 2; ++q) {
+                int t = lane + 32 * q;
+                bool hit = (t < m) && COL(i, t) == jc;
+                unsigned hm = __ballot_sync(kFull, hit);
+                if (hm && tpos < 0) tpos = 32 * q + __ffs(hm) - 1;
+            }
+            if (tpos < 0) return 5;
+            const long long hh = CST(i, tpos) - v[jc] - mn;
+            bool eq[2];
+            int jq[2];
+            for (int q = 0; q < 2; ++q) {
+                int t = lane + 32 * q;
+                eq[q] = false;
+                jq[q] = -1;
+                if (t < m) {
+                    int j = COL(i, t);
+                    jq[q] = j;
+                    if (!ok[j]) {
+                        long long vj = CST(i, t) - hh - v[j];
+                        if (vj < dd[j]) {
+                            dd[j] = vj;
+                            lab[j] = i;
+                            eq[q] = (vj == mn);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            for (int q = 0; q < 2 && jend < 0; ++q) {
+                bool isf = eq[q] && y[jq[q]] < 0;
+                unsigned em = __ballot_sync(kFull, eq[q]), fm = __ballot_sync(kFull, isf);
+                unsigned upto = em;
+                if (fm) {
+                    int fl = __ffs(fm) - 1;
+                    upto = em & ((1u << fl) - 1u);
+                    jend = __shfl_sync(kFull, jq[q], fl);
+                    price = true;
+                }
+                if (eq[q] && ((upto >> lane) & 1u)) {
+                    todo[k + __popc(upto & ltmask)] = jq[q];
+                    ok[jq[q]] = 1;
+                }
+                k += __popc(upto);
+            }
+            __syncwarp();
+            if (jend >= 0) break;
+            if (k != 0) continue;
+            long long lm = kLLMax;
+            for (int j = lane; j < n; j += 32)
+                if (!ok[j] && dd[j] <= kBigInt - 1 && dd[j] < lm) lm = dd[j];
+            lm = wmin_ll(lm);
+            if (lm == kLLMax) { mn = kBigInt - 1; k = 0; continue; }
+            mn = lm;
+            for (int b = 0; b < n; b += 32) {
+                int j = b + lane;
+                bool sel = (j < n) && !ok[j] && dd[j] == mn;
+                unsigned sm = __ballot_sync(kFull, sel);
+                if (sel) todo[k + __popc(sm & ltmask)] = j;
+                k += __popc(sm);
+            }
+            __syncwarp();
+            for (int b = 0; b < k && jend < 0; b += 32) {
+                int h = b + lane, j = (h < k) ? todo[h] : -1;
+                bool fre = (h < k) && y[j] < 0;
+                unsigned fm = __ballot_sync(kFull, fre);
+                if (fm) {
+                    int first = b + __ffs(fm) - 1;
+                    if (h < first) ok[j] = 1;
+                    jend = todo[first];
+                    price = true;
+                } else if (h < k) {
+                    ok[j] = 1;
+                }
+            }
+            __syncwarp();
+        }
         if (price && mn != 0)
-            for (int q = td + 1; q < n; ++q) {
+            for (int q = td + 1 + lane; q < n; q += 32) {
                 int jj = todo[q];
                 v[jj] += dd[jj] - mn;
             }
-        for (int steps = 0;; ++steps) {
-            if (steps > n + 1) return 6;
-            int i = lab[jend];
-            y[jend] = i;
-            int ks = jend;
-            jend = x[i];
-            x[i] = ks;
-            if (i == i0) break;
+        __syncwarp();
+        int fail = 0;
+        if (lane == 0) {
+            int je = jend;
+            for (int steps = 0;; ++steps) {
+                if (steps > n + 1) { fail = 1; break; }
+                int i = lab[je];
+                y[je] = i;
+                int ks = je;
+                je = x[i];
+                x[i] = ks;
+                if (i == i0) break;
+            }
         }
+        if (__shfl_sync(kFull, fail, 0)) return 6;
+        __syncwarp();
     }
     return 0;
 }
 
-__device__ inline double pairdist2(const double *c1, const double *c2, int bulk, const double *box) {
-    double d = 0;
+__device__ __forceinline__ double wsum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+template <typename DT>
+__device__ __forceinline__ DT pdist2(const DT *c1, const DT *c2, int bulk, const double *box) {
+    DT d = 0;
     for (int k = 0; k < 3; ++k) {
-        double t = c1[k] - c2[k];
+        DT t = c1[k] - c2[k];
         if (bulk) {
             if (box[k] == 0.0) continue;
-            t -= box[k] * round(t / box[k]);
+            DT bk = (DT)box[k];
+            t -= bk * round(t / bk);
         }
         d += t * t;
     }
     return d;
 }
 
-struct RefineCtl {
-    double Rb[9], Rc[9], Rn[9], cmb[3], db[3], dn[3], d0[3];
-    double newdist, pdsum;
-    int nperm, ntries, fail, done;
-};
+// The m nearest columns of one row as the binary max-heap of PAIRDISTS
+// (alignutils.f90:641-701): the first m columns are sifted up in order, each
+// later closer column replaces the root and is sifted down.  The heap's array
+// order is the stored order of the row.
+template <typename DT, typename KT>
+__device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, const DT *bi, const DT *acol, int ns, int m,
+                                             int bulk, const double *box) {
+    for (int j = 0; j < m; ++j) {
+        hd[j] = pdist2<DT>(bi, acol + 3 * j, bulk, box);
+        hk[j] = (KT)j;
+        int l = j + 1;
+        while (l > 1) {
+            int l2 = l / 2;
+            if (hd[l2 - 1] < hd[l - 1]) {
+                DT h = hd[l2 - 1]; hd[l2 - 1] = hd[l - 1]; hd[l - 1] = h;
+                KT t = hk[l2 - 1]; hk[l2 - 1] = hk[l - 1]; hk[l - 1] = t;
+                l = l2;
+            } else break;
+        }
+    }
+    for (int j = m; j < ns; ++j) {
+        DT d = pdist2<DT>(bi, acol + 3 * j, bulk, box);
+        if (!(d < hd[0])) continue;
+        hd[0] = d;
+        hk[0] = (KT)j;
+        int l = 1;
+        for (int guard = 0; guard < 64; ++guard) {
+            int l2 = 2 * l;
+            if (l2 + 1 > m) {
+                if (l2 <= m && hd[l2 - 1] > hd[l - 1]) {
+                    DT h = hd[l2 - 1]; hd[l2 - 1] = hd[l - 1]; hd[l - 1] = h;
+                    KT t = hk[l2 - 1]; hk[l2 - 1] = hk[l - 1]; hk[l - 1] = t;
+                }
+                break;
+            }
+            int a = (hd[l2] > hd[l2 - 1]) ? l2 + 1 : l2;
+            if (hd[a - 1] > hd[l - 1]) {
+                DT h = hd[a - 1]; hd[a - 1] = hd[l - 1]; hd[l - 1] = h;
+                KT t = hk[a - 1]; hk[a - 1] = hk[l - 1]; hk[l - 1] = t;
+                l = a;
+            } else break;
+        }
+    }
+}
 
-__global__ void __launch_bounds__(256) k_refine(const PairDev *pairs, const GroupDev *groups,
-                                                const int *cand2pair, const double *xa,
-                                                const double *xb, const double *peaks,
-                                                const int *npeaks, unsigned char *lap,
-                                                double *cdist, double *cR, double *cdisp,
-                                                double *cxyz, int *cperm, int *cniter, int *cstat) {
-    extern __shared__ double sm[];
-    __shared__ RefineCtl C;
-    __shared__ double red[32 * 10];
-    const int c = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+// ---------------------------------------------------------------------------
+// ITERATIVEALIGN from one candidate, executed by one warp (block of 32).
+template <typename DT, typename CT>
+__global__ void __launch_bounds__(32) k_refine_warp(
+    const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
+    const double *xa, const double *xb, const double *peaks, const int *npeaks, unsigned char *lapg,
+    double *cdist, double *cR, double *cdisp, double *cxyz, int *cperm, int *cniter, int *cstat) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double sRb[9], sRn[9], sRc[9];
+    const int lane = threadIdx.x;
+    const int c = cand_list[blockIdx.x];
     const int p = cand2pair[c];
     const PairDev &P = pairs[p];
     const int local = c - P.cand0, o = local / P.nrot, ci = local % P.nrot;
     if (ci >= npeaks[2 * p + o]) {
-        if (tid == 0) { cdist[c] = INFINITY; cstat[c] = -1; }
+        if (lane == 0) { cdist[c] = INFINITY; cstat[c] = -1; }
         return;
     }
     const int n = P.n, bulk = P.bulk, a0 = P.atom0;
-    double *DB = sm, *A0 = DB + 3 * n, *DA = A0 + 3 * n, *DUM = DA + 3 * n;
-    int *permbest = (int *)(DUM + 3 * n), *saveperm = permbest + n, *newperm = saveperm + n;
+    int maxg = 0;
+    for (int gi = 0; gi < P.ngroups; ++gi) maxg = max(maxg, groups[P.group0 + gi].n);
+    RefLayout L;
+    ref_layout(n, maxg, sizeof(DT) == 4, (int)sizeof(CT), L);
+    double *DB = (double *)(smem + L.DB), *A0 = (double *)(smem + L.A0), *DA = (double *)(smem + L.DA);
+    DT *DBf = (DT *)(smem + L.DBf), *DAf = (DT *)(smem + L.DAf);
+    int *permbest = (int *)(smem + L.perm), *newperm = (int *)(smem + L.nperm), *ptmp = (int *)(smem + L.ptmp);
+    unsigned char *lb = P.lapstride ? lapg + P.lap0 + (long long)local * P.lapstride : smem + L.coord_end;
+    CT *lcc = (CT *)(lb + L.lap_cc);
+    unsigned short *lkk = (unsigned short *)(lb + L.lap_kk);
+    long long *lv = (long long *)(lb + L.lap_v), *ld = (long long *)(lb + L.lap_d);
+    int *lx = (int *)(lb + L.lap_x), *ly = (int *)(lb + L.lap_y), *llab = (int *)(lb + L.lap_lab);
+    int *lfr = (int *)(lb + L.lap_fr), *ltodo = (int *)(lb + L.lap_todo);
+    unsigned char *lok = lb + L.lap_ok;
     const double box[3] = {P.box[0], P.box[1], P.box[2]};
     const double *pk = peaks + 3LL * (P.cand0 + o * P.nrot + ci);
-    if (tid == 0) {
-        for (int k = 0; k < 9; ++k) C.Rb[k] = (k % 4 == 0) ? 1.0 : 0.0;
-        for (int k = 0; k < 3; ++k) { C.db[k] = 0; C.cmb[k] = 0; C.d0[k] = 0; }
-        if (bulk) {
-            for (int k = 0; k < 9; ++k) C.Rc[k] = (k % 4 == 0) ? 1.0 : 0.0;
-            for (int k = 0; k < 3; ++k) C.d0[k] = (pk[k] - 1.0) * box[k] / P.G;
-        } else {
+    double d0[3] = {0, 0, 0};
+    if (lane == 0) {
+        for (int k = 0; k < 9; ++k) { sRb[k] = (k % 4 == 0) ? 1.0 : 0.0; sRc[k] = sRb[k]; }
+        if (!bulk) {
             const double conv = FO_PI / P.G;
-            euler_matrix((pk[0] - 1.0) * 2 * conv, (pk[1] - 0.5) * conv, (pk[2] - 1.0) * 2 * conv, C.Rc);
+            euler_matrix((pk[0] - 1.0) * 2 * conv, (pk[1] - 0.5) * conv, (pk[2] - 1.0) * 2 * conv, sRc);
         }
-        C.fail = 0;
     }
-    __syncthreads();
+    if (bulk)
+        for (int k = 0; k < 3; ++k) d0[k] = (pk[k] - 1.0) * box[k] / P.G;
+    __syncwarp();
     const double sgn = (o == 1) ? -1.0 : 1.0;
     double cs[6] = {0, 0, 0, 0, 0, 0};
-    for (int j = tid; j < n; j += nt) {
+    for (int j = lane; j < n; j += 32) {
         const double *a = xa + 3LL * (a0 + j), *b = xb + 3LL * (a0 + j);
         for (int k = 0; k < 3; ++k) DB[3 * j + k] = b[k];
         if (bulk) {
-            for (int k = 0; k < 3; ++k) A0[3 * j + k] = a[k] - C.d0[k];
+            for (int k = 0; k < 3; ++k) A0[3 * j + k] = a[k] - d0[k];
         } else {
             for (int k = 0; k < 3; ++k)
-                A0[3 * j + k] = sgn * (C.Rc[3 * k] * a[0] + C.Rc[3 * k + 1] * a[1] + C.Rc[3 * k + 2] * a[2]);
+                A0[3 * j + k] = sgn * (sRc[3 * k] * a[0] + sRc[3 * k + 1] * a[1] + sRc[3 * k + 2] * a[2]);
         }
         for (int k = 0; k < 3; ++k) { cs[k] += A0[3 * j + k]; cs[3 + k] += DB[3 * j + k]; }
     }
-    block_sum<double, 6>(cs, red);
+    for (int k = 0; k < 6; ++k) cs[k] = wsum_d(cs[k]);
+    double cmb[3] = {0, 0, 0};
+    __syncwarp();
     if (!bulk) {  // ITERATIVEALIGN works on structures centred at their centroids
-        for (int j = tid; j < n; j += nt)
+        for (int k = 0; k < 3; ++k) cmb[k] = cs[3 + k] / n;
+        for (int j = lane; j < n; j += 32)
             for (int k = 0; k < 3; ++k) {
                 A0[3 * j + k] -= cs[k] / n;
-                DB[3 * j + k] -= cs[3 + k] / n;
+                DB[3 * j + k] -= cmb[k];
             }
-        if (tid == 0)
-            for (int k = 0; k < 3; ++k) C.cmb[k] = cs[3 + k] / n;
     }
-    for (int j = tid; j < n; j += nt) {
-        for (int k = 0; k < 3; ++k) DA[3 * j + k] = A0[3 * j + k];
+    __syncwarp();
+    for (int j = lane; j < n; j += 32) {
+        for (int k = 0; k < 3; ++k) {
+            DA[3 * j + k] = A0[3 * j + k];
+            if (sizeof(DT) == 4) { DAf[3 * j + k] = (DT)A0[3 * j + k]; DBf[3 * j + k] = (DT)DB[3 * j + k]; }
+        }
         permbest[j] = j;
     }
-    if (tid == 0) { C.ntries = 0; C.nperm = n; C.done = 0; }
-    __syncthreads();
-    const int maxg_m = 0;
-    (void)maxg_m;
-    unsigned char *lapbase = lap + P.lap0 + (long long)local * P.lapstride;
-    int maxg = 0;
-    for (int gi = 0; gi < P.ngroups; ++gi) maxg = max(maxg, groups[P.group0 + gi].n);
-    LapView LV = lap_view(lapbase, maxg);
-
-    for (int iter = 0; iter < 64 && C.nperm > 0; ++iter) {
-        for (int j = tid; j < n; j += nt) {
-            for (int k = 0; k < 3; ++k) DUM[3 * j + k] = DA[3 * j + k];
-            saveperm[j] = permbest[j];
-            newperm[j] = j;
-        }
-        if (tid == 0) C.pdsum = 0;
-        __syncthreads();
+    __syncwarp();
+    double db[3] = {0, 0, 0}, newdist = 0;
+    int ntries = 0, nperm = n, fail = 0;
+    for (int iter = 0; iter < 64 && nperm > 0; ++iter) {
+        for (int j = lane; j < n; j += 32) newperm[j] = j;
+        double pdsum = 0;
+        __syncwarp();
         for (int gi = 0; gi < P.ngroups; ++gi) {
             const GroupDev g = groups[P.group0 + gi];
             const int ns = g.n, m = g.m, s0 = g.slot0 - a0;
-            for (int i = tid; i < ns; i += nt) {
-                const double *bi = DB + 3 * (s0 + i);
-                long long *crow = LV.cc + (long long)i * m;
-                int *krow = LV.kk + (long long)i * m;
-                if (m == ns) {
-                    for (int j = 0; j < ns; ++j) {
-                        crow[j] = (long long)(pairdist2(bi, DA + 3 * (s0 + j), bulk, box) * kPScale);
-                        krow[j] = j;
-                    }
+            const bool dense = (m == ns);
+            for (int i = lane; i < ns; i += 32) {
+                const DT *bi = DBf + 3 * (s0 + i);
+                CT *crow = lcc + (long long)i * m;
+                if (dense) {
+                    for (int j = 0; j < ns; ++j)
+                        crow[j] = (CT)((double)pdist2<DT>(bi, DAf + 3 * (s0 + j), bulk, box) * kPScale);
+                } else if (sizeof(DT) == 4 && sizeof(CT) == 4) {
+                    // heap kept in place: float distances in the 32-bit cost slots
+                    float *hd = reinterpret_cast<float *>(crow);
+                    unsigned short *hk = lkk + (long long)i * m;
+                    nearest_heap<float, unsigned short>(hd, hk, (const float *)bi, (const float *)DAf + 3 * s0,
+                                                        ns, m, bulk, box);
+                    for (int j = 0; j < m; ++j) crow[j] = (CT)((double)hd[j] * kPScale);
                 } else {
-                    double hd[kMaxNei];
+                    DT hd[kMaxNei];
                     int hk[kMaxNei];
+                    nearest_heap<DT, int>(hd, hk, bi, DAf + 3 * s0, ns, m, bulk, box);
+                    unsigned short *krow = lkk + (long long)i * m;
                     for (int j = 0; j < m; ++j) {
-                        hd[j] = pairdist2(bi, DA + 3 * (s0 + j), bulk, box);
-                        hk[j] = j;
-                        int l = j + 1;
-                        while (l > 1) {
-                            int l2 = l / 2;
-                            if (hd[l2 - 1] < hd[l - 1]) {
-                                double h = hd[l2 - 1]; hd[l2 - 1] = hd[l - 1]; hd[l - 1] = h;
-                                int t = hk[l2 - 1]; hk[l2 - 1] = hk[l - 1]; hk[l - 1] = t;
-                                l = l2;
-                            } else break;
-                        }
-                    }
-                    for (int j = m; j < ns; ++j) {
-                        double d = pairdist2(bi, DA + 3 * (s0 + j), bulk, box);
-                        if (!(d < hd[0])) continue;
-                        hd[0] = d;
-                        hk[0] = j;
-                        int l = 1;
-                        for (int guard = 0; guard < 64; ++guard) {
-                            int l2 = 2 * l;
-                            if (l2 + 1 > m) {
-                                if (l2 <= m && hd[l2 - 1] > hd[l - 1]) {
-                                    double h = hd[l2 - 1]; hd[l2 - 1] = hd[l - 1]; hd[l - 1] = h;
-                                    int t = hk[l2 - 1]; hk[l2 - 1] = hk[l - 1]; hk[l - 1] = t;
-                                }
-                                break;
-                            }
-                            int a = (hd[l2] > hd[l2 - 1]) ? l2 + 1 : l2;
-                            if (hd[a - 1] > hd[l - 1]) {
-                                double h = hd[a - 1]; hd[a - 1] = hd[l - 1]; hd[l - 1] = h;
-                                int t = hk[a - 1]; hk[a - 1] = hk[l - 1]; hk[l - 1] = t;
-                                l = a;
-                            } else break;
-                        }
-                    }
-                    for (int j = 0; j < m; ++j) {
-                        crow[j] = (long long)(hd[j] * kPScale);
-                        krow[j] = hk[j];
+                        crow[j] = (CT)((double)hd[j] * kPScale);
+                        krow[j] = (unsigned short)hk[j];
                     }
                 }
             }
-            __syncthreads();
-            if (tid == 0) {
-                int rc = jv_sparse(ns, m, LV.cc, LV.kk, LV);
-                if (rc) C.fail += 1;
-                double pd = 0;
-                for (int i = 0; i < ns; ++i) {
-                    int col = LV.x[i];
-                    if (col >= ns) { col = ns - 1; C.fail += 1; }
-                    if (col < 0) { col = 0; C.fail += 1; }
-                    newperm[s0 + i] = s0 + col;
-                    pd += pairdist2(DB + 3 * (s0 + i), DA + 3 * (s0 + col), bulk, box);
-                }
-                C.pdsum += pd;
+            __syncwarp();
+            int rc = jv_warp<CT>(ns, m, dense, lcc, lkk, lv, ld, lx, ly, llab, lfr, ltodo, lok);
+            if (rc) fail += 1;
+            __syncwarp();
+            for (int i = lane; i < ns; i += 32) {
+                int col = lx[i];
+                if (col >= ns) { col = ns - 1; fail += 1; }
+                if (col < 0) { col = 0; fail += 1; }
+                newperm[s0 + i] = s0 + col;
+                pdsum += pdist2<double>(DB + 3 * (s0 + i), DA + 3 * (s0 + col), bulk, box);
             }
-            __syncthreads();
+            __syncwarp();
         }
-        int cnt[1] = {0};
-        for (int j = tid; j < n; j += nt) {
+        pdsum = wsum_d(pdsum);
+        int cnt = 0;
+        for (int j = lane; j < n; j += 32) {
             int q = newperm[j];
-            for (int k = 0; k < 3; ++k) DA[3 * j + k] = DUM[3 * q + k];
-            permbest[j] = saveperm[q];
-            if (q != j) ++cnt[0];
+            ptmp[j] = permbest[q];
+            if (q != j) ++cnt;
         }
-        block_sum<int, 1>(cnt, (int *)red);
+        for (int o2 = 16; o2 > 0; o2 >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o2);
         if (bulk) {
             double s3[3] = {0, 0, 0};
-            for (int j = tid; j < n; j += nt)
+            for (int j = lane; j < n; j += 32) {
+                const double *a = DA + 3 * newperm[j];
                 for (int k = 0; k < 3; ++k) {
-                    double t = DB[3 * j + k] - DA[3 * j + k];
+                    double t = DB[3 * j + k] - a[k];
                     s3[k] += t - box[k] * round(t / box[k]);
                 }
-            block_sum<double, 3>(s3, red);
-            double dn[3] = {s3[0] / n, s3[1] / n, s3[2] / n};
-            double s1[1] = {0};
-            for (int j = tid; j < n; j += nt) {
-                double a[3] = {DA[3 * j] + dn[0], DA[3 * j + 1] + dn[1], DA[3 * j + 2] + dn[2]};
-                s1[0] += pairdist2(DB + 3 * j, a, 1, box);
             }
-            block_sum<double, 1>(s1, red);
-            if (tid == 0) {
-                C.newdist = sqrt(s1[0]);
-                for (int k = 0; k < 3; ++k) C.db[k] += dn[k];
+            double dn[3];
+            for (int k = 0; k < 3; ++k) dn[k] = wsum_d(s3[k]) / n;
+            double s1 = 0;
+            for (int j = lane; j < n; j += 32) {
+                const double *a = DA + 3 * newperm[j];
+                double ad[3] = {a[0] + dn[0], a[1] + dn[1], a[2] + dn[2]};
+                s1 += pdist2<double>(DB + 3 * j, ad, 1, box);
             }
-            __syncthreads();
-            for (int j = tid; j < n; j += nt)
-                for (int k = 0; k < 3; ++k) DA[3 * j + k] = A0[3 * permbest[j] + k] + C.db[k];
+            newdist = sqrt(wsum_d(s1));
+            for (int k = 0; k < 3; ++k) db[k] += dn[k];
+            __syncwarp();
+            for (int j = lane; j < n; j += 32) {
+                permbest[j] = ptmp[j];
+                for (int k = 0; k < 3; ++k) {
+                    DA[3 * j + k] = A0[3 * ptmp[j] + k] + db[k];
+                    if (sizeof(DT) == 4) DAf[3 * j + k] = (DT)DA[3 * j + k];
+                }
+            }
         } else {
             double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-            for (int j = tid; j < n; j += nt) {
-                const double *b = DB + 3 * j, *a = DA + 3 * j;
+            for (int j = lane; j < n; j += 32) {
+                const double *b = DB + 3 * j, *a = DA + 3 * newperm[j];
                 double xm = b[0] - a[0], ym = b[1] - a[1], zm = b[2] - a[2];
                 double xp = b[0] + a[0], yp = b[1] + a[1], zp = b[2] + a[2];
                 q[0] += xm * xm + ym * ym + zm * zm;
@@ -436,53 +586,52 @@ __global__ void __launch_bounds__(256) k_refine(const PairDev *pairs, const Grou
                 q[8] += ym * zm - yp * zp;
                 q[9] += xp * xp + yp * yp + zm * zm;
             }
-            block_sum<double, 10>(q, red);
-            if (tid == 0) {
-                C.newdist = kearsley_rotation(q, C.Rn);
-                matmul3(C.Rn, C.Rb, C.Rb);
+            for (int k = 0; k < 10; ++k) q[k] = wsum_d(q[k]);
+            if (lane == 0) {
+                newdist = kearsley_rotation(q, sRn);
+                matmul3(sRn, sRb, sRb);
             }
-            __syncthreads();
-            for (int j = tid; j < n; j += nt) {
-                const double *a = A0 + 3 * permbest[j];
-                for (int k = 0; k < 3; ++k)
-                    DA[3 * j + k] = C.Rb[3 * k] * a[0] + C.Rb[3 * k + 1] * a[1] + C.Rb[3 * k + 2] * a[2];
+            newdist = __shfl_sync(kFull, newdist, 0);
+            __syncwarp();
+            for (int j = lane; j < n; j += 32) {
+                permbest[j] = ptmp[j];
+                const double *a = A0 + 3 * ptmp[j];
+                for (int k = 0; k < 3; ++k) {
+                    DA[3 * j + k] = sRb[3 * k] * a[0] + sRb[3 * k + 1] * a[1] + sRb[3 * k + 2] * a[2];
+                    if (sizeof(DT) == 4) DAf[3 * j + k] = (DT)DA[3 * j + k];
+                }
             }
         }
-        if (tid == 0) {
-            C.nperm = cnt[0];
-            C.ntries += 1;
-            double pd = sqrt(C.pdsum);
-            if ((C.newdist - pd) / C.newdist > sqrt((double)n) / kPScale) C.done = 1;
-            if (C.ntries > kMaxTries) C.done = 1;
-            if (C.done) C.nperm = 0;
-        }
-        __syncthreads();
+        __syncwarp();
+        nperm = cnt;
+        ntries += 1;
+        double pd = sqrt(pdsum);
+        if ((newdist - pd) / newdist > sqrt((double)n) / kPScale) nperm = 0;
+        if (ntries > kMaxTries) nperm = 0;
     }
-    // final minimisation
+    // final minimisation without a new permutation
     if (bulk) {
         double s3[3] = {0, 0, 0};
-        for (int j = tid; j < n; j += nt)
+        for (int j = lane; j < n; j += 32)
             for (int k = 0; k < 3; ++k) {
                 double t = DB[3 * j + k] - DA[3 * j + k];
                 s3[k] += t - box[k] * round(t / box[k]);
             }
-        block_sum<double, 3>(s3, red);
-        double dn[3] = {s3[0] / n, s3[1] / n, s3[2] / n};
-        double s1[1] = {0};
-        for (int j = tid; j < n; j += nt) {
-            double a[3] = {DA[3 * j] + dn[0], DA[3 * j + 1] + dn[1], DA[3 * j + 2] + dn[2]};
-            s1[0] += pairdist2(DB + 3 * j, a, 1, box);
+        double dn[3];
+        for (int k = 0; k < 3; ++k) dn[k] = wsum_d(s3[k]) / n;
+        double s1 = 0;
+        for (int j = lane; j < n; j += 32) {
+            double ad[3] = {DA[3 * j] + dn[0], DA[3 * j + 1] + dn[1], DA[3 * j + 2] + dn[2]};
+            s1 += pdist2<double>(DB + 3 * j, ad, 1, box);
         }
-        block_sum<double, 1>(s1, red);
-        for (int j = tid; j < n; j += nt)
+        newdist = sqrt(wsum_d(s1));
+        for (int k = 0; k < 3; ++k) db[k] += dn[k];
+        __syncwarp();
+        for (int j = lane; j < n; j += 32)
             for (int k = 0; k < 3; ++k) DA[3 * j + k] += dn[k];
-        if (tid == 0) {
-            C.newdist = sqrt(s1[0]);
-            for (int k = 0; k < 3; ++k) C.db[k] += dn[k];
-        }
     } else {
         double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int j = tid; j < n; j += nt) {
+        for (int j = lane; j < n; j += 32) {
             const double *b = DB + 3 * j, *a = DA + 3 * j;
             double xm = b[0] - a[0], ym = b[1] - a[1], zm = b[2] - a[2];
             double xp = b[0] + a[0], yp = b[1] + a[1], zp = b[2] + a[2];
@@ -497,32 +646,34 @@ __global__ void __launch_bounds__(256) k_refine(const PairDev *pairs, const Grou
             q[8] += ym * zm - yp * zp;
             q[9] += xp * xp + yp * yp + zm * zm;
         }
-        block_sum<double, 10>(q, red);
-        if (tid == 0) {
-            C.newdist = kearsley_rotation(q, C.Rn);
-            matmul3(C.Rn, C.Rb, C.Rb);
+        for (int k = 0; k < 10; ++k) q[k] = wsum_d(q[k]);
+        if (lane == 0) {
+            newdist = kearsley_rotation(q, sRn);
+            matmul3(sRn, sRb, sRb);
         }
-        __syncthreads();
-        for (int j = tid; j < n; j += nt) {
+        newdist = __shfl_sync(kFull, newdist, 0);
+        __syncwarp();
+        for (int j = lane; j < n; j += 32) {
             double a[3] = {DA[3 * j], DA[3 * j + 1], DA[3 * j + 2]};
             for (int k = 0; k < 3; ++k)
-                DA[3 * j + k] = C.Rn[3 * k] * a[0] + C.Rn[3 * k + 1] * a[1] + C.Rn[3 * k + 2] * a[2] + C.cmb[k];
+                DA[3 * j + k] = sRn[3 * k] * a[0] + sRn[3 * k + 1] * a[1] + sRn[3 * k + 2] * a[2] + cmb[k];
         }
     }
-    __syncthreads();
+    __syncwarp();
     const long long ob = P.candatom0 + (long long)local * n;
-    for (int j = tid; j < n; j += nt) {
+    for (int j = lane; j < n; j += 32) {
         cperm[ob + j] = permbest[j];
         for (int k = 0; k < 3; ++k) cxyz[3 * (ob + j) + k] = DA[3 * j + k];
     }
-    if (tid == 0) {
-        cdist[c] = C.newdist;
+    for (int o2 = 16; o2 > 0; o2 >>= 1) fail += __shfl_xor_sync(kFull, fail, o2);
+    if (lane == 0) {
+        cdist[c] = newdist;
         double R[9];
-        matmul3(C.Rb, C.Rc, R);
+        matmul3(sRb, sRc, R);
         for (int k = 0; k < 9; ++k) cR[9LL * c + k] = bulk ? ((k % 4 == 0) ? 1.0 : 0.0) : R[k];
-        for (int k = 0; k < 3; ++k) cdisp[3LL * c + k] = C.db[k] - C.d0[k];
-        cniter[c] = C.ntries;
-        cstat[c] = C.fail ? (int)ST_LAP_FAILED : 0;
+        for (int k = 0; k < 3; ++k) cdisp[3LL * c + k] = db[k] - d0[k];
+        cniter[c] = ntries;
+        cstat[c] = fail ? (int)ST_LAP_FAILED : 0;
     }
 }
 
@@ -588,15 +739,37 @@ __global__ void k_select(const PairDev *pairs, const int *slot2orig, const int *
     }
 }
 
-long long lap_bytes_host(int maxg) { return lap_bytes(maxg); }
 
-size_t refine_smem_bytes(int maxn) { return (size_t)maxn * (12 * sizeof(double) + 3 * sizeof(int)); }
-
-void launch_refine(const RefineBuffers &b, cudaStream_t s) {
-    size_t sm = refine_smem_bytes(b.maxn);
-    cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_refine<<<b.ncand, 256, sm, s>>>(b.pairs, b.groups, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks,
-                                      b.lap, b.cdist, b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);
+// Buckets run concurrently on the auxiliary streams (fork/join through
+// events on the main stream) so that small and large problems share the SMs.
+void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,
+                   cudaEvent_t fork, cudaEvent_t *join) {
+    cudaEventRecord(fork, main);
+    for (int a = 0; a < naux; ++a) cudaStreamWaitEvent(aux[a], fork, 0);
+    for (int k = 0; k < b.nbuckets; ++k) {
+        const RefineBucket &bk = b.buckets[k];
+        if (bk.count == 0) continue;
+        const int *list = b.cand_list + bk.offset;
+        cudaStream_t s = naux ? aux[k % naux] : main;
+#define FO_LAUNCH_REFINE(DT, CT)                                                                   \
+    do {                                                                                          \
+        cudaFuncSetAttribute(k_refine_warp<DT, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                             (int)bk.smem);                                                       \
+        k_refine_warp<DT, CT><<<bk.count, 32, bk.smem, s>>>(                                      \
+            b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,  \
+            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);                                   \
+    } while (0)
+        if (b.fp32) {
+            if (bk.ct64) FO_LAUNCH_REFINE(float, long long); else FO_LAUNCH_REFINE(float, int);
+        } else {
+            if (bk.ct64) FO_LAUNCH_REFINE(double, long long); else FO_LAUNCH_REFINE(double, int);
+        }
+#undef FO_LAUNCH_REFINE
+    }
+    for (int a = 0; a < naux; ++a) {
+        cudaEventRecord(join[a], aux[a]);
+        cudaStreamWaitEvent(main, join[a], 0);
+    }
 }
 
 void launch_select(const RefineBuffers &b, cudaStream_t s) {

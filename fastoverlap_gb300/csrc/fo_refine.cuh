@@ -1,0 +1,48 @@
+// fo_refine.cuh -- shared-memory / scratch layout of one refinement
+// candidate, computed identically on the host (bucketing) and the device.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fo {
+
+struct RefLayout {
+    size_t DB, A0, DA, DBf, DAf, perm, nperm, ptmp, coord_end;
+    size_t lap_cc, lap_kk, lap_v, lap_d, lap_x, lap_y, lap_lab, lap_fr, lap_todo, lap_ok, lap_end;
+};
+
+__host__ __device__ inline size_t ref_a16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// n atoms, largest permutation group maxg, FP32 distance copies when fp32,
+// ctsize = bytes per integer cost (4 or 8).
+__host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsize, RefLayout &L) {
+    size_t o = 0;
+    L.DB = o; o += ref_a16(24 * (size_t)n);
+    L.A0 = o; o += ref_a16(24 * (size_t)n);
+    L.DA = o; o += ref_a16(24 * (size_t)n);
+    if (fp32) {
+        L.DBf = o; o += ref_a16(12 * (size_t)n);
+        L.DAf = o; o += ref_a16(12 * (size_t)n);
+    } else {
+        L.DBf = L.DB;
+        L.DAf = L.DA;
+    }
+    L.perm = o; o += ref_a16(4 * (size_t)n);
+    L.nperm = o; o += ref_a16(4 * (size_t)n);
+    L.ptmp = o; o += ref_a16(4 * (size_t)n);
+    L.coord_end = o;
+    const int m = maxg < 60 ? maxg : 60;
+    size_t p = 0;
+    L.lap_cc = p; p += ref_a16((size_t)ctsize * maxg * m);
+    L.lap_kk = p; p += (maxg > 60) ? ref_a16(2 * (size_t)maxg * m) : 0;
+    L.lap_v = p; p += ref_a16(8 * (size_t)maxg);
+    L.lap_d = p; p += ref_a16(8 * (size_t)maxg);
+    L.lap_x = p; p += ref_a16(4 * (size_t)maxg);
+    L.lap_y = p; p += ref_a16(4 * (size_t)maxg);
+    L.lap_lab = p; p += ref_a16(4 * (size_t)maxg);
+    L.lap_fr = p; p += ref_a16(4 * (size_t)maxg);
+    L.lap_todo = p; p += ref_a16(4 * (size_t)maxg);
+    L.lap_ok = p; p += ref_a16((size_t)maxg);
+    L.lap_end = p;
+}
+
+}  // namespace fo

@@ -873,14 +873,17 @@ static double orc_findbestperm(const double *B, const double *A, int n, const in
 static void orc_jacobi4(double a[4][4], double w[4], double V[4][4]) {
     for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 4; ++j) V[i][j] = (i == j);
+    /* an off-diagonal element below 1e-17 sqrt(|a_pp a_qq|) is zero at double
+     * precision: zero it; a sweep without rotations ends the iteration */
     for (int sweep = 0; sweep < 64; ++sweep) {
-        double off = 0;
-        for (int p = 0; p < 4; ++p)
-            for (int q = p + 1; q < 4; ++q) off += a[p][q] * a[p][q];
-        if (off == 0.0) break;
+        int rotated = 0;
         for (int p = 0; p < 4; ++p)
             for (int q = p + 1; q < 4; ++q) {
-                if (a[p][q] == 0.0) continue;
+                if (fabs(a[p][q]) <= 1e-17 * sqrt(fabs(a[p][p] * a[q][q]))) {
+                    a[p][q] = a[q][p] = 0.0;
+                    continue;
+                }
+                rotated = 1;
                 double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
                 double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
                 double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
@@ -900,6 +903,7 @@ static void orc_jacobi4(double a[4][4], double w[4], double V[4][4]) {
                     V[k][q] = s * vkp + c * vkq;
                 }
             }
+        if (!rotated) break;
     }
     for (int i = 0; i < 4; ++i) w[i] = a[i][i];
 }
