@@ -254,4 +254,121 @@ __host__ __device__ inline double kearsley_rotation(const double *q, double *R) 
     return sqrt(minv);
 }
 
+// Smallest eigenpair of the Kearsley matrix with few FP64 operations:
+// cyclic Jacobi on the matrix scaled to unit norm in FP32 gives an
+// approximate eigenvector v0; in FP64 the Rayleigh quotient lambda of v0 and
+// one inverse-iteration step (Q - lambda I) x = v0 (Gaussian elimination with
+// partial pivoting) bring it to double precision -- the error contracts by
+// |lambda - lambda_min| / gap, and lambda is already accurate to O(|v0
+// error|^2).  Returns the distance sqrt(lambda_min) and R as
+// kearsley_rotation does.
+__host__ __device__ inline double kearsley_rotation_fast(const double *q, double *R) {
+    const double Q[4][4] = {{q[0], q[1], q[2], q[3]},
+                            {q[1], q[4], q[5], q[6]},
+                            {q[2], q[5], q[7], q[8]},
+                            {q[3], q[6], q[8], q[9]}};
+    double nrm = 0;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) nrm = fmax(nrm, fabs(Q[i][j]));
+    if (!(nrm > 0.0)) {
+        for (int k = 0; k < 9; ++k) R[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        return 0.0;
+    }
+    float a[4][4], V[4][4];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            a[i][j] = (float)(Q[i][j] / nrm);
+            V[i][j] = (i == j) ? 1.f : 0.f;
+        }
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        int rotated = 0;
+        for (int p = 0; p < 4; ++p)
+            for (int r = p + 1; r < 4; ++r) {
+                if (fabsf(a[p][r]) <= 1e-8f * sqrtf(fabsf(a[p][p] * a[r][r])) || fabsf(a[p][r]) < 1e-30f) {
+                    a[p][r] = a[r][p] = 0.f;
+                    continue;
+                }
+                rotated = 1;
+                float theta = (a[r][r] - a[p][p]) / (2.f * a[p][r]);
+                float t = (theta >= 0 ? 1.f : -1.f) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+                float c = 1.f / sqrtf(t * t + 1.f), s = t * c;
+                for (int k = 0; k < 4; ++k) {
+                    float akp = a[k][p], akr = a[k][r];
+                    a[k][p] = c * akp - s * akr;
+                    a[k][r] = s * akp + c * akr;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    float apk = a[p][k], ark = a[r][k];
+                    a[p][k] = c * apk - s * ark;
+                    a[r][k] = s * apk + c * ark;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    float vkp = V[k][p], vkr = V[k][r];
+                    V[k][p] = c * vkp - s * vkr;
+                    V[k][r] = s * vkp + c * vkr;
+                }
+            }
+        if (!rotated) break;
+    }
+    int jmin = 0;
+    for (int j = 1; j < 4; ++j)
+        if (a[j][j] < a[jmin][jmin]) jmin = j;
+    double v[4] = {V[0][jmin], V[1][jmin], V[2][jmin], V[3][jmin]};
+    auto rayleigh = [&](const double *x) {
+        double num = 0, den = 0;
+        for (int i = 0; i < 4; ++i) {
+            double qi = 0;
+            for (int j = 0; j < 4; ++j) qi += Q[i][j] * x[j];
+            num += x[i] * qi;
+            den += x[i] * x[i];
+        }
+        return num / den;
+    };
+    double lam = rayleigh(v);
+    // one step of inverse iteration on (Q - lam I)
+    double M[4][5];
+    for (int i = 0; i < 4; ++i) {
+        for (int j = 0; j < 4; ++j) M[i][j] = Q[i][j] - (i == j ? lam : 0.0);
+        M[i][4] = v[i];
+    }
+    const double tiny = 1e-300 + 1e-18 * nrm;
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int i = c + 1; i < 4; ++i)
+            if (fabs(M[i][c]) > fabs(M[piv][c])) piv = i;
+        if (piv != c)
+            for (int j = 0; j < 5; ++j) { double t = M[c][j]; M[c][j] = M[piv][j]; M[piv][j] = t; }
+        if (fabs(M[c][c]) < tiny) M[c][c] = (M[c][c] < 0 ? -tiny : tiny);
+        double inv = 1.0 / M[c][c];
+        for (int i = c + 1; i < 4; ++i) {
+            double f = M[i][c] * inv;
+            for (int j = c; j < 5; ++j) M[i][j] -= f * M[c][j];
+        }
+    }
+    double x[4];
+    for (int i = 3; i >= 0; --i) {
+        double t = M[i][4];
+        for (int j = i + 1; j < 4; ++j) t -= M[i][j] * x[j];
+        x[i] = t / M[i][i];
+    }
+    double xn = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3]);
+    if (xn > 0.0 && isfinite(xn)) {
+        for (int i = 0; i < 4; ++i) v[i] = x[i] / xn;
+        lam = rayleigh(v);
+    }
+    double minv = lam;
+    if (minv < 0.0) minv = (fabs(minv) < 1e-6) ? 0.0 : -minv;
+    double q1 = v[0], q2 = v[1], q3 = v[2], q4 = v[3];
+    R[0] = q1 * q1 + q2 * q2 - q3 * q3 - q4 * q4;
+    R[1] = 2 * (q2 * q3 + q1 * q4);
+    R[2] = 2 * (q2 * q4 - q1 * q3);
+    R[3] = 2 * (q2 * q3 - q1 * q4);
+    R[4] = q1 * q1 + q3 * q3 - q2 * q2 - q4 * q4;
+    R[5] = 2 * (q3 * q4 + q1 * q2);
+    R[6] = 2 * (q2 * q4 + q1 * q3);
+    R[7] = 2 * (q3 * q4 - q1 * q2);
+    R[8] = q1 * q1 + q4 * q4 - q2 * q2 - q3 * q3;
+    return sqrt(minv);
+}
+
 }  // namespace fo

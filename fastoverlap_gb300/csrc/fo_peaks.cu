@@ -14,19 +14,20 @@ namespace fo {
 constexpr int kMaxWin = 7;  // largest window half-width handled on chip
 constexpr int kPeakThreads = 64;
 
+template <typename T>
 struct LMShared {
-    double H[66];   // packed lower triangle of J^T J
-    double g[11];   // J^T r
-    double A[66];   // Cholesky factor
-    double dl[11];  // step
-    double p[11];
-    double pn[11];
+    T H[66];   // packed lower triangle of J^T J
+    T g[11];   // J^T r
+    T A[66];   // Cholesky factor
+    T dl[11];  // step
+    T p[11];
+    T pn[11];
     int info;
     int ok;
 };
 
-template <typename T>
-__device__ inline T peak_model(const double *p, T u1, T u2, T u3, T *e_out) {
+template <typename T, typename P>
+__device__ inline T peak_model(const P *p, T u1, T u2, T u3, T *e_out) {
     T Y = T(p[2]) * u1 * u1 + T(p[3]) * u2 * u2 + T(p[4]) * u3 * u3 + T(p[5]) * u1 * u2 +
           T(p[6]) * u2 * u3 + T(p[7]) * u1 * u3;
     T e = exp(-Y);
@@ -36,12 +37,12 @@ __device__ inline T peak_model(const double *p, T u1, T u2, T u3, T *e_out) {
 
 // sum of squared residuals over the window (every lane gets the total)
 template <typename T>
-__device__ T lm_cost(const double *p, const T *win, int w) {
+__device__ T lm_cost(const T *p, const T *win, int w) {
     const int n = 2 * w + 1, npts = n * n * n, lane = threadIdx.x & 31;
     T S = 0;
     for (int i = lane; i < npts; i += 32) {
         int i1 = i % n, i2 = (i / n) % n, i3 = i / (n * n);
-        T r = peak_model<T>(p, T(i1 + 1 - p[8]), T(i2 + 1 - p[9]), T(i3 + 1 - p[10]), (T *)nullptr) - win[i];
+        T r = peak_model<T, T>(p, T(i1 + 1) - p[8], T(i2 + 1) - p[9], T(i3 + 1) - p[10], (T *)nullptr) - win[i];
         S += r * r;
     }
     return warp_sum(S);
@@ -51,12 +52,15 @@ __device__ T lm_cost(const double *p, const T *win, int w) {
 // lambda /10 after an accepted step, *10 after a rejected one; stop when the
 // relative decrease or the relative step is <= tol (info 1/2/3), when lambda
 // exceeds 1e16 (info 4) or after maxfev model evaluations (info 5).
-// Executed by one full warp; S holds the shared state.
+// Executed by one full warp in the precision T of the grid; the damped
+// normal equations are solved by lane 0 (Cholesky; in FP32 after scaling the
+// system to unit diagonal, which leaves the step unchanged).
 template <typename T>
-__device__ int lm_fit_warp(LMShared &S, const T *win, int w, double tol) {
+__device__ int lm_fit_warp(LMShared<T> &S, const T *win, int w, T tol) {
     const int lane = threadIdx.x & 31, n = 2 * w + 1, npts = n * n * n, maxfev = 1200;
-    double lambda = 1e-3;
-    double cost = (double)lm_cost<T>(S.p, win, w);
+    constexpr bool kScale = sizeof(T) == 4;
+    T lambda = T(1e-3);
+    T cost = lm_cost<T>(S.p, win, w);
     int nfev = 1;
     if (!isfinite(cost)) return 0;
     for (int outer = 0; outer < 100000; ++outer) {
@@ -65,16 +69,16 @@ __device__ int lm_fit_warp(LMShared &S, const T *win, int w, double tol) {
         for (int q = 0; q < 77; ++q) h[q] = 0;
         for (int i = lane; i < npts; i += 32) {
             int i1 = i % n, i2 = (i / n) % n, i3 = i / (n * n);
-            T u1 = T(i1 + 1 - S.p[8]), u2 = T(i2 + 1 - S.p[9]), u3 = T(i3 + 1 - S.p[10]), e;
-            T f = peak_model<T>(S.p, u1, u2, u3, &e);
+            T u1 = T(i1 + 1) - S.p[8], u2 = T(i2 + 1) - S.p[9], u3 = T(i3 + 1) - S.p[10], e;
+            T f = peak_model<T, T>(S.p, u1, u2, u3, &e);
             T r = f - win[i];
-            T ae = T(S.p[0]) * e, J[11];
+            T ae = S.p[0] * e, J[11];
             J[0] = e; J[1] = 1;
             J[2] = -ae * u1 * u1; J[3] = -ae * u2 * u2; J[4] = -ae * u3 * u3;
             J[5] = -ae * u1 * u2; J[6] = -ae * u2 * u3; J[7] = -ae * u1 * u3;
-            J[8] = ae * (T(2 * S.p[2]) * u1 + T(S.p[5]) * u2 + T(S.p[7]) * u3);
-            J[9] = ae * (T(2 * S.p[3]) * u2 + T(S.p[5]) * u1 + T(S.p[6]) * u3);
-            J[10] = ae * (T(2 * S.p[4]) * u3 + T(S.p[6]) * u2 + T(S.p[7]) * u1);
+            J[8] = ae * (T(2) * S.p[2] * u1 + S.p[5] * u2 + S.p[7] * u3);
+            J[9] = ae * (T(2) * S.p[3] * u2 + S.p[5] * u1 + S.p[6] * u3);
+            J[10] = ae * (T(2) * S.p[4] * u3 + S.p[6] * u2 + S.p[7] * u1);
             int q = 0;
 #pragma unroll
             for (int a = 0; a < 11; ++a)
@@ -86,61 +90,70 @@ __device__ int lm_fit_warp(LMShared &S, const T *win, int w, double tol) {
 #pragma unroll
         for (int q = 0; q < 77; ++q) h[q] = warp_sum(h[q]);
         if (lane == 0) {
-            for (int q = 0; q < 66; ++q) S.H[q] = (double)h[q];
-            for (int a = 0; a < 11; ++a) S.g[a] = (double)h[66 + a];
+            for (int q = 0; q < 66; ++q) S.H[q] = h[q];
+            for (int a = 0; a < 11; ++a) S.g[a] = h[66 + a];
         }
         __syncwarp();
         for (int inner = 0; inner < 64; ++inner) {
             if (lane == 0) {
-                // A = H + lambda diag(H); Cholesky in packed storage
                 int ok = 1;
+                T sc[11];
+                for (int a = 0; a < 11; ++a) {
+                    T dgl = S.H[a * (a + 1) / 2 + a];
+                    sc[a] = kScale ? T(1) / sqrt(dgl > T(1e-30) ? dgl : T(1e-30)) : T(1);
+                }
+                // A = S (H + lambda diag(H)) S with S = diag(sc); packed Cholesky
                 for (int a = 0, q = 0; a < 11; ++a)
                     for (int b = 0; b <= a; ++b, ++q) {
-                        double v = S.H[q];
-                        if (a == b) v += lambda * fmax(S.H[q], 1e-30);
-                        S.A[q] = v;
+                        T v = S.H[q];
+                        if (a == b) v += lambda * (S.H[q] > T(1e-30) ? S.H[q] : T(1e-30));
+                        S.A[q] = v * sc[a] * sc[b];
                     }
-                double inv[11];
+                T inv[11];
                 for (int j = 0; j < 11 && ok; ++j) {
                     int jj = j * (j + 1) / 2;
-                    double s = S.A[jj + j];
+                    T s = S.A[jj + j];
                     for (int k = 0; k < j; ++k) s -= S.A[jj + k] * S.A[jj + k];
-                    if (!(s > 0.0)) { ok = 0; break; }
-                    double djj = sqrt(s);
-                    inv[j] = 1.0 / djj;
+                    if (!(s > T(0))) { ok = 0; break; }
+                    T djj = sqrt(s);
+                    inv[j] = T(1) / djj;
                     S.A[jj + j] = djj;
                     for (int i = j + 1; i < 11; ++i) {
                         int ii = i * (i + 1) / 2;
-                        double t = S.A[ii + j];
+                        T t = S.A[ii + j];
                         for (int k = 0; k < j; ++k) t -= S.A[ii + k] * S.A[jj + k];
                         S.A[ii + j] = t * inv[j];
                     }
                 }
                 if (ok) {
-                    double y[11];
+                    T y[11];
                     for (int i = 0; i < 11; ++i) {
                         int ii = i * (i + 1) / 2;
-                        double t = -S.g[i];
+                        T t = -S.g[i] * sc[i];
                         for (int k = 0; k < i; ++k) t -= S.A[ii + k] * y[k];
                         y[i] = t * inv[i];
                     }
                     for (int i = 10; i >= 0; --i) {
-                        double t = y[i];
+                        T t = y[i];
                         for (int k = i + 1; k < 11; ++k) t -= S.A[k * (k + 1) / 2 + i] * S.dl[k];
                         S.dl[i] = t * inv[i];
                     }
-                    for (int a = 0; a < 11; ++a) S.pn[a] = S.p[a] + S.dl[a];
+                    for (int a = 0; a < 11; ++a) {
+                        S.dl[a] *= sc[a];
+                        S.pn[a] = S.p[a] + S.dl[a];
+                    }
                 }
                 S.ok = ok;
             }
             __syncwarp();
-            double cn = INFINITY;
-            if (S.ok) {
-                cn = (double)lm_cost<T>(S.pn, win, w);
+            T cn = T(INFINITY);
+            const int okk = S.ok;
+            if (okk) {
+                cn = lm_cost<T>(S.pn, win, w);
                 ++nfev;
             }
-            if (S.ok && cn < cost) {
-                double rel = (cost - cn) / cost, step = 0, pnorm = 0;
+            if (okk && cn < cost) {
+                T rel = (cost - cn) / cost, step = 0, pnorm = 0;
                 for (int a = 0; a < 11; ++a) {
                     step += S.dl[a] * S.dl[a];
                     pnorm += S.pn[a] * S.pn[a];
@@ -152,7 +165,7 @@ __device__ int lm_fit_warp(LMShared &S, const T *win, int w, double tol) {
                     for (int a = 0; a < 11; ++a) S.p[a] = S.pn[a];
                 __syncwarp();
                 cost = cn;
-                lambda = fmax(lambda * 0.1, 1e-15);
+                lambda = lambda * T(0.1) > T(1e-15) ? lambda * T(0.1) : T(1e-15);
                 bool c1 = rel <= tol, c2 = step <= tol * (pnorm + tol);
                 if (c1 && c2) return 3;
                 if (c1) return 1;
@@ -160,8 +173,8 @@ __device__ int lm_fit_warp(LMShared &S, const T *win, int w, double tol) {
                 if (nfev >= maxfev) return 5;
                 break;
             }
-            lambda *= 10.0;
-            if (lambda > 1e16) return 4;
+            lambda *= T(10);
+            if (lambda > T(1e16)) return 4;
             if (nfev >= maxfev) return 5;
             __syncwarp();
         }
@@ -214,7 +227,7 @@ __device__ void subtract_argmax_sum(T *f, int G, const double *pp, double c1, do
     int bi = N;
     double s = 0;
     for (; i < N; i += step) {
-        T v = f[i] - peak_model<T>(pp, T(i1 + 1 - c1), T(i2 + 1 - c2), T(i3 + 1 - c3), (T *)nullptr);
+        T v = f[i] - peak_model<T, double>(pp, T(i1 + 1 - c1), T(i2 + 1 - c2), T(i3 + 1 - c3), (T *)nullptr);
         f[i] = v;
         s += (double)v;
         if (v > best) { best = v; bi = i; }
@@ -248,7 +261,7 @@ template <typename T>
 __global__ void __launch_bounds__(kPeakThreads) k_findpeaks(const PairDev *pairs, T *grids, double *omax,
                                                    double *peaks, int *npeaks, int *pstatus,
                                                    double tol) {
-    __shared__ LMShared S;
+    __shared__ LMShared<T> S;
     __shared__ T win[(2 * kMaxWin + 1) * (2 * kMaxWin + 1) * (2 * kMaxWin + 1)];
     __shared__ double sred[32];
     __shared__ T vred[32];
@@ -280,18 +293,18 @@ __global__ void __launch_bounds__(kPeakThreads) k_findpeaks(const PairDev *pairs
             }
             if (threadIdx.x == 0) {
                 double init[11] = {(double)mx - mean, mean, 1, 1, 1, 0, 0, 0, width + 1.0, width + 1.0, width + 1.0};
-                for (int a = 0; a < 11; ++a) S.p[a] = init[a];
+                for (int a = 0; a < 11; ++a) S.p[a] = T(init[a]);
             }
             __syncthreads();
             if (threadIdx.x < 32) {
-                int info = lm_fit_warp<T>(S, win, width, tol);
+                int info = lm_fit_warp<T>(S, win, width, T(tol));
                 if (threadIdx.x == 0) s_info = info;
             }
             __syncthreads();
             const int info = s_info;
             if (info == 0 || info == 5) break;
-            const double c1 = S.p[8] - width - 1 + (a1 + 1), c2 = S.p[9] - width - 1 + (a2 + 1),
-                         c3 = S.p[10] - width - 1 + (a3 + 1);
+            const double c1 = (double)S.p[8] - width - 1 + (a1 + 1), c2 = (double)S.p[9] - width - 1 + (a2 + 1),
+                         c3 = (double)S.p[10] - width - 1 + (a3 + 1);
             if (threadIdx.x == 0) {
                 pk[3 * nfound] = c1;
                 pk[3 * nfound + 1] = c2;
@@ -301,7 +314,7 @@ __global__ void __launch_bounds__(kPeakThreads) k_findpeaks(const PairDev *pairs
             // subtract the fitted peak (not wrapped) and its mean level; the same
             // pass finds the next first maximum and the new grid sum
             double pp[11];
-            for (int a = 0; a < 11; ++a) pp[a] = S.p[a];
+            for (int a = 0; a < 11; ++a) pp[a] = (double)S.p[a];
             __syncthreads();
             subtract_argmax_sum<T>(f, G, pp, c1, c2, c3, mx, amax, sum, sred, vred, ired);
         }

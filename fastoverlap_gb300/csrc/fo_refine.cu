@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(32) k_refine_warp(
             }
             for (int k = 0; k < 10; ++k) q[k] = wsum_d(q[k]);
             if (lane == 0) {
-                newdist = kearsley_rotation(q, sRn);
+                newdist = kearsley_rotation_fast(q, sRn);
                 matmul3(sRn, sRb, sRb);
             }
             newdist = __shfl_sync(kFull, newdist, 0);
@@ -648,7 +648,7 @@ __global__ void __launch_bounds__(32) k_refine_warp(
         }
         for (int k = 0; k < 10; ++k) q[k] = wsum_d(q[k]);
         if (lane == 0) {
-            newdist = kearsley_rotation(q, sRn);
+            newdist = kearsley_rotation_fast(q, sRn);
             matmul3(sRn, sRb, sRb);
         }
         newdist = __shfl_sync(kFull, newdist, 0);
