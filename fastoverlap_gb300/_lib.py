@@ -98,6 +98,11 @@ EXPORTS = {
     "fo_profile_reset": (None, [_vp]),
     "fo_cluster_overlap": (ctypes.c_int, [_vp, _vp, _dp, _dp, _ip, _ip, ctypes.c_int, _dp, _dp]),
     "fo_bulk_overlap": (ctypes.c_int, [_vp, _vp, _dp, _dp, _ip, _ip, ctypes.c_int, _dp]),
+    "fo_bulk_overlap_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _ip, ctypes.c_int,
+                                                ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_int, ctypes.c_int, _vp,
+                                                _vp]),
+    "fo_bulk_overlap_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "fo_ctx_record": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fo_ctx_elapsed_ms": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_float)]),

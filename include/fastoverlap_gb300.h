@@ -170,6 +170,29 @@ fo_status fo_bulk_overlap(fo_ctx *ctx, const fo_bulk_pair *pair, const double *p
                           const double *pos2, const int *perm, const int *group_sizes,
                           int index_base, double *grid);
 
+/* ---- periodic overlap grid without device allocation ----
+ * No counterpart in the reference.  For callers that cannot let a library
+ * allocate device memory (their own pool owns it, or an allocation in the
+ * middle of a request is not allowed): same result as fo_bulk_overlap in
+ * FP64, but inputs and output are DEVICE pointers and the only scratch is a
+ * fixed file-scope device array (fo_bulk_overlap_noalloc_scratch_bytes(),
+ * about 4 MiB, held by every GPU that loads the library until exit).
+ * Limits: nfspace (M) <= 64, at most 64 permutation groups; larger requests
+ * return FO_ERR_BAD_ARGS.  The atoms of group g must be the contiguous range
+ * [sum of earlier sizes, + group_sizes[g]) of d_pos1/d_pos2 (3 doubles each);
+ * group_sizes is a host array.  d_grid receives M^3 doubles, x fastest.
+ * Work is queued on `stream` (a cudaStream_t, NULL = default stream) and the
+ * call returns without waiting.  The first call on a device looks up the
+ * scratch array's address; make that first call before any stream capture.
+ * All calls share the array (it keeps the previous contents; the kernel
+ * clears what must start at zero): calls that overlap on the GPU race and
+ * must be serialised by the caller.                                          */
+fo_status fo_bulk_overlap_noalloc(const double *d_pos1, const double *d_pos2, int natoms,
+                                  const int *group_sizes, int ngroups, double boxlx,
+                                  double boxly, double boxlz, double kwidth, int nwave,
+                                  int nfspace, double *d_grid, void *stream);
+size_t    fo_bulk_overlap_noalloc_scratch_bytes(void);
+
 /* ---- Fortran-compatible single-pair entry points ----
  * fo_setperm keeps the permutation groups in the context, as SETPERM keeps
  * them in module storage; permgroup is 1-based like the Fortran array.      */
