@@ -1024,11 +1024,6 @@ fo_status fo_ctx_flush_l2(fo_ctx *ctx, size_t bytes) {
     cudaSetDevice(ctx->opts.device);
     if (bytes > ctx->flush_bytes) {
         cudaFree(ctx->flush_buf);
-    for (int a = 0; a < fo_ctx::kAux; ++a) {
-        if (ctx->aux[a]) cudaStreamDestroy(ctx->aux[a]);
-        if (ctx->join[a]) cudaEventDestroy(ctx->join[a]);
-    }
-    if (ctx->fork) cudaEventDestroy(ctx->fork);
         ctx->flush_buf = nullptr;
         ctx->flush_bytes = 0;
         fo_status s = cuda_check(ctx, cudaMalloc(&ctx->flush_buf, bytes), "cudaMalloc(flush)");

@@ -83,3 +83,25 @@ def test_bad_arguments_raise(fo):
         fo.SphericalAlign(0.3, 7).align_full(A, B)
     with pytest.raises(fo.FoError):
         fo.PeriodicAlignFortran(10, [0.0, 1.0, 1.0]).align(A, A)              # zero box length
+
+
+def test_plan_runs_after_l2_flush_and_events(fo):
+    """Benchmark helpers (L2 flush, event timing) leave the context usable."""
+    ps = synth.config2(6, seed_offset=31)
+    ctx = fo.Context(precision="mixed", profile=True)
+    b = fo.ClusterBatch(ctx, [p["pos1"] for p in ps], [p["pos2"] for p in ps],
+                        [p["perm"] for p in ps], Jmax=[p["Jmax"] for p in ps], scale=0.3,
+                        nrot=10).plan()
+    b.plan_run()
+    b.plan_wait()
+    first = b.plan_results(False)["dist"]
+    for _ in range(2):
+        ctx.flush_l2(64 << 20)
+        ctx.record(0)
+        b.plan_run()
+        ctx.record(1)
+        b.plan_wait()
+        assert ctx.elapsed_ms(0, 1) > 0
+    assert np.array_equal(b.plan_results(False)["dist"], first)
+    assert "refine" in ctx.profile()
+    b.close()
