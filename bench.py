@@ -339,7 +339,7 @@ def main():
             "frac": achieved / hbm, "traffic": None, "peak_source": peak_src,
             "kernel_ms_per_launch": top_ms,
             "kernel_share": kern[top][0] / sum(v[0] for v in kern.values())}
-    launches = sum(v[1] for v in kern.values())
+    launches = batch.plan_launches() * args.steps
 
     cpu = None
     if not args.no_cpu_baseline:

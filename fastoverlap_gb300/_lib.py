@@ -83,6 +83,7 @@ EXPORTS = {
     "fo_plan_wait": (ctypes.c_int, [_vp]),
     "fo_plan_results": (ctypes.c_int, [_vp, _dp, _ip, _vp]),
     "fo_plan_device_bytes": (ctypes.c_size_t, [_vp]),
+    "fo_plan_launches": (ctypes.c_int, [_vp]),
     "fo_plan_destroy": (None, [_vp]),
     "fo_setperm": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, ctypes.c_int]),
     "fo_get_bestperm": (ctypes.c_int, [_vp, _ip]),

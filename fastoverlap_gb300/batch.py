@@ -112,6 +112,10 @@ class _BatchBase(object):
     def plan_device_bytes(self):
         return int(self.ctx.lib.fo_plan_device_bytes(self.plan_h))
 
+    def plan_launches(self):
+        """Kernel launches one plan_run issues."""
+        return int(self.ctx.lib.fo_plan_launches(self.plan_h))
+
     def close(self):
         if self.plan_h is not None:
             self.ctx.lib.fo_plan_destroy(self.plan_h)

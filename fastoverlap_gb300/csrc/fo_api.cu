@@ -792,6 +792,15 @@ fo_status fo_plan_results(fo_plan *pl, double *aligned, int *permbest, fo_pair_r
 
 size_t fo_plan_device_bytes(const fo_plan *pl) { return pl ? pl->dbytes : 0; }
 
+int fo_plan_launches(const fo_plan *pl) {
+    if (!pl) return 0;
+    int nb = 0;
+    for (const auto &b : pl->buckets) nb += b.count > 0;
+    // cluster: centre, ylm, radial, coeff, isoft; bulk: prep, sf, 3 fft passes;
+    // then findpeaks, one refinement launch per bucket, select
+    return (pl->bulk ? 5 : 5) + 1 + nb + 1;
+}
+
 void fo_plan_destroy(fo_plan *pl) {
     if (!pl) return;
     cudaSetDevice(pl->ctx->opts.device);

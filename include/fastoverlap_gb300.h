@@ -151,6 +151,7 @@ fo_status fo_plan_wait(fo_plan *plan);
 fo_status fo_plan_results(fo_plan *plan, double *aligned, int *permbest,
                           fo_pair_result *results);
 size_t    fo_plan_device_bytes(const fo_plan *plan);
+int       fo_plan_launches(const fo_plan *plan);   /* kernel launches per fo_plan_run */
 void      fo_plan_destroy(fo_plan *plan);
 
 /* ---- stage outputs of one pair (parity checks, diagnostics) ----
