@@ -211,16 +211,18 @@ struct RefAssign {
 // Shared-memory footprint of one refinement warp for a pair, and whether its
 // assignment arrays fit on chip.  dmax bounds every atom-atom distance the
 // refinement can meet; costs INT(d^2 1e6) below 2e9 are held in 32 bits.
-RefAssign ref_assign(int n, int maxg, bool fp32, double dmax) {
+// recomp: costs recomputed from FP32 coordinates instead of stored.
+RefAssign ref_assign(int n, int maxg, bool fp32, bool recomp, double dmax) {
     RefAssign r;
     r.ct64 = (dmax * dmax * fo::kPScale >= 2.0e9) ? 1 : 0;
     fo::RefLayout L;
-    fo::ref_layout(n, maxg, fp32, r.ct64 ? 8 : 4, L);
-    auto up = [](size_t b) {   // coarse classes keep the number of concurrent launches small
-        const size_t cls[] = {16384, 32768, 49152, 65536, 81920, 98304, 131072, 163840, 196608, 229376};
-        for (size_t c : cls)
-            if (b <= c) return c;
-        return (b + 4095) & ~(size_t)4095;
+    fo::ref_layout(n, maxg, fp32, r.ct64 ? 8 : 4, recomp, L);
+    // Footprint classes: one launch per class.  Steps of 2 KB up to 16 KB, 4 KB
+    // up to 48 KB and 16 KB beyond keep the rounding (and so the loss of
+    // resident warps per SM) small where most candidates fall.
+    auto up = [](size_t b) {
+        const size_t step = b <= 16384 ? 2048 : (b <= 49152 ? 4096 : 16384);
+        return (b + step - 1) / step * step;
     };
     if (L.coord_end + L.lap_end <= kRefSmemCap) {
         r.smem = up(L.coord_end + L.lap_end);
@@ -492,6 +494,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     r.buckets = pl->buckets.data();
     r.nbuckets = (int)pl->buckets.size();
     r.fp32 = pl->fp32;
+    r.recomp = pl->fp32 && !pl->bulk;
     pl->d_pstatus = r.pstatus;
     pl->d_npeaks = r.npeaks;
     return FO_OK;
@@ -565,7 +568,7 @@ fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair 
         }
         {
             double dmax = centred_radius(pos1 + 3 * q.coord_off, n) + centred_radius(pos2 + 3 * q.coord_off, n);
-            RefAssign ra = ref_assign(n, maxg, pl->fp32, dmax);
+            RefAssign ra = ref_assign(n, maxg, pl->fp32, pl->fp32, dmax);
             P.lapstride = ra.lapstride;
             P.lap0 = lap_total;
             lap_total += (long long)P.norient * P.nrot * P.lapstride;
@@ -676,7 +679,7 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
         }
         {
             double dmax = 0.5 * std::sqrt(q.box[0] * q.box[0] + q.box[1] * q.box[1] + q.box[2] * q.box[2]);
-            RefAssign ra = ref_assign(n, maxg, pl->fp32, dmax);
+            RefAssign ra = ref_assign(n, maxg, pl->fp32, false, dmax);
             P.lapstride = ra.lapstride;
             P.lap0 = lap_total;
             lap_total += (long long)P.nrot * P.lapstride;

@@ -76,6 +76,7 @@ struct RefineBuffers {
     const RefineBucket *buckets;   // host
     int nbuckets;
     bool fp32;
+    bool recomp;   // costs recomputed from FP32 coordinates (mixed cluster form)
 };
 void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s);
 void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,

@@ -182,18 +182,41 @@ __device__ int lm_fit_warp(LMShared<T> &S, const T *win, int w, T tol) {
     return 5;
 }
 
+// Per-thread running sum of a grid: FP64 for FP64 grids; for FP32 grids a
+// compensated (Kahan) FP32 sum, which keeps about FP64 accuracy over the few
+// thousand terms a thread adds without issuing FP64 instructions in the grid
+// loop.  Partial sums are combined across threads in FP64.
+template <typename T>
+struct GridSum {
+    double s = 0;
+    __device__ void add(T v) { s += (double)v; }
+    __device__ double get() const { return s; }
+};
+template <>
+struct GridSum<float> {
+    float s = 0, c = 0;
+    __device__ void add(float v) {
+        const float y = v - c, t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ double get() const { return (double)s - (double)c; }
+};
+
 // block-wide (max value, first index) and sum over a grid; all threads get it
 template <typename T>
-__device__ void block_argmax_sum(const T *f, long long N, T &mx, long long &amax, double &sum,
+__device__ void block_argmax_sum(const T *f, int N, T &mx, long long &amax, double &sum,
                                  double *sred, T *vred, long long *ired) {
     T best = -INFINITY;
-    long long bi = N;
-    double s = 0;
-    for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+    int bl = N;
+    GridSum<T> acc;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
         T v = f[i];
-        s += (double)v;
-        if (v > best) { best = v; bi = i; }
+        acc.add(v);
+        if (v > best) { best = v; bl = i; }
     }
+    long long bi = bl;
+    double s = acc.get();
     // warp level
     for (int o = 16; o > 0; o >>= 1) {
         T ov = __shfl_xor_sync(0xffffffffu, best, o);
@@ -223,19 +246,25 @@ __device__ void subtract_argmax_sum(T *f, int G, const double *pp, double c1, do
     const int N = G * G * G, step = blockDim.x;
     int i = threadIdx.x, i1 = i % G, i2 = (i / G) % G, i3 = i / (G * G);
     const int d1 = step % G, d2 = (step / G) % G, d3 = step / (G * G);
+    // the model is evaluated in the grid's precision T
+    T pt[11];
+#pragma unroll
+    for (int a = 0; a < 11; ++a) pt[a] = T(pp[a]);
+    const T t1 = T(c1), t2 = T(c2), t3 = T(c3);
     T best = -INFINITY;
     int bi = N;
-    double s = 0;
+    GridSum<T> acc;
     for (; i < N; i += step) {
-        T v = f[i] - peak_model<T, double>(pp, T(i1 + 1 - c1), T(i2 + 1 - c2), T(i3 + 1 - c3), (T *)nullptr);
+        T v = f[i] - peak_model<T, T>(pt, T(i1 + 1) - t1, T(i2 + 1) - t2, T(i3 + 1) - t3, (T *)nullptr);
         f[i] = v;
-        s += (double)v;
+        acc.add(v);
         if (v > best) { best = v; bi = i; }
         i1 += d1; i2 += d2; i3 += d3;
         if (i1 >= G) { i1 -= G; ++i2; }
         if (i2 >= G) { i2 -= G; ++i3; }
     }
     long long bl = bi;
+    double s = acc.get();
     for (int o = 16; o > 0; o >>= 1) {
         T ov = __shfl_xor_sync(0xffffffffu, best, o);
         long long oi = __shfl_xor_sync(0xffffffffu, bl, o);
@@ -276,7 +305,7 @@ __global__ void __launch_bounds__(kPeakThreads) k_findpeaks(const PairDev *pairs
     T mx;
     long long amax;
     double sum;
-    block_argmax_sum<T>(f, N, mx, amax, sum, sred, vred, ired);
+    block_argmax_sum<T>(f, (int)N, mx, amax, sum, sred, vred, ired);
     if (threadIdx.x == 0) omax[2 * p + o] = (double)mx;
     int width = 2, nfound = 0;
     double *pk = peaks + 3LL * (P.cand0 + o * P.nrot);

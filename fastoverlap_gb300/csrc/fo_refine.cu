@@ -10,6 +10,10 @@
 // Candidates are launched in buckets of equal shared-memory footprint so
 // small problems pack many warps per SM; the assignment arrays live in
 // shared memory when they fit and in per-candidate global scratch otherwise.
+// In the mixed-precision cluster form the costs are not stored: the
+// assignment recomputes each one from the FP32 coordinates (float4 per atom)
+// where it reads it, which keeps the per-warp footprint small enough for
+// many warps per SM.
 //
 // Reference behaviour (matthewghgriffiths/fastoverlap):
 //   ITERATIVEALIGN   fastoverlap/f90/alignutils.f90:111-286
@@ -26,18 +30,86 @@
 #include "fo_kernels.h"
 #include "fo_refine.cuh"
 
+#include <cstdint>
+
 namespace fo {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr long long kLLMax = 0x7fffffffffffffffLL;
+constexpr unsigned long long kNoKey = ~0ull;
+// Row scans order entries by the key ((h + kKeyBias) << 6) | t: reduced cost
+// h first, scan position t (< 64) second.  Reduced costs are >= 0 (column
+// prices only decrease from the column minima) and below BIGINT = 1e12 <
+// 2^40 where they enter a key, so the key is exact and below 2^63.
+constexpr long long kKeyBias = 1LL << 56;
 
-__device__ __forceinline__ long long wmin_ll(long long v) {
-    for (int o = 16; o > 0; o >>= 1) {
-        long long w = __shfl_xor_sync(kFull, v, o);
-        v = w < v ? w : v;
-    }
-    return v;
+// Warp minimum of a 64-bit unsigned key: redux on the high words, then on
+// the low words of the lanes holding the minimal high word.
+__device__ __forceinline__ unsigned long long wmin_u64(unsigned long long k) {
+    const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    const unsigned mh = __reduce_min_sync(kFull, hi);
+    const unsigned ml = __reduce_min_sync(kFull, hi == mh ? lo : 0xffffffffu);
+    return ((unsigned long long)mh << 32) | ml;
 }
+
+// Warp minimum of a signed 64-bit value (sign bit flipped: unsigned order).
+__device__ __forceinline__ long long wmin_ll(long long v) {
+    const unsigned long long s = 0x8000000000000000ull;
+    return (long long)(wmin_u64((unsigned long long)v ^ s) ^ s);
+}
+
+// ---------------------------------------------------------------------------
+// Squared distances and integer costs in FP32 (mixed form).  Every rounding
+// is explicit so that a distance recomputed anywhere equals the one the
+// neighbour heap ordered.
+__device__ __forceinline__ float d2_f4(const float4 p, const float4 q) {
+    const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y), dz = __fsub_rn(p.z, q.z);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// minimum image along one axis of length bk (no wrap when bk == 0)
+__device__ __forceinline__ float min_image_f(float t, float bk) {
+    return bk != 0.f ? __fsub_rn(t, __fmul_rn(bk, roundf(__fdiv_rn(t, bk)))) : t;
+}
+
+__device__ __forceinline__ float d2_f4_box(const float4 p, const float4 q, const float *bx) {
+    const float dx = min_image_f(__fsub_rn(p.x, q.x), bx[0]);
+    const float dy = min_image_f(__fsub_rn(p.y, q.y), bx[1]);
+    const float dz = min_image_f(__fsub_rn(p.z, q.z), bx[2]);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// INT(d2 * 1e6) of an FP32 squared distance d2 >= 0, equal to truncating the
+// FP64 product (double)d2 * 1e6, without FP64 instructions.  1e6 is exact in
+// FP32 and the product splits exactly into hi + lo (hi the rounded FP32
+// product, lo its FMA residual).  When hi is an integer the floor of hi + lo
+// is hi + floor(lo); otherwise |lo| <= ulp(hi)/2 keeps hi + lo strictly
+// between the two integers around hi, so it is floor(hi).  CT = int needs
+// d2 * 1e6 < 2^31.
+template <typename CT>
+__device__ __forceinline__ CT cost_of_f32(float d2) {
+    const float hi = __fmul_rn(d2, 1.0e6f);
+    const float lo = __fmaf_rn(d2, 1.0e6f, -hi);
+    const float fh = floorf(hi);
+    if (fh == hi) return (CT)hi + (CT)floorf(lo);
+    return (CT)fh;
+}
+
+// Cost of row i, scan position t, column j.
+template <typename CT>
+struct CostStored {      // costs kept in a row-major table of width m
+    const CT *cc;
+    int m;
+    __device__ __forceinline__ long long operator()(int i, int t, int) const { return (long long)cc[i * m + t]; }
+};
+
+template <typename CT>
+struct CostF32 {         // cluster costs recomputed from FP32 coordinates
+    const float4 *b, *a;
+    __device__ __forceinline__ long long operator()(int i, int, int j) const {
+        return (long long)cost_of_f32<CT>(d2_f4(b[i], a[j]));
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Sparse Jonker-Volgenant (Computing 38, 1987) executed by one warp.  The
@@ -49,29 +121,44 @@ __device__ __forceinline__ long long wmin_ll(long long v) {
 // column in scan / index order ends a path).  Only the scans inside a step
 // (a row's <= 60 entries, or all columns) are spread over the 32 lanes, so
 // the assignment is the one the sequential method produces.  Rows have a
-// fixed width m; dense rows (m == n) have implicit column index t.  All
-// lanes must call; returns 0 on success, > 0 when the matching fails.
-template <typename CT>
-__device__ int jv_warp(const int n, const int m, const bool dense, const CT *__restrict__ cc,
-                       const unsigned short *__restrict__ kk, long long *v, long long *dd, int *x,
-                       int *y, int *lab, int *fr, int *todo, unsigned char *ok) {
+// fixed width m <= 60; dense rows (m == n) have implicit column index t,
+// sparse rows the column indices kk.  All lanes must call; returns 0 on
+// success, > 0 when the matching fails.
+template <typename KT, typename CF>
+__device__ int jv_warp(const int n, const int m, const bool dense, const CF &cost, const KT *__restrict__ kk,
+                       long long *v, long long *dd, int *x, int *y, int *lab, int *fr, int *todo,
+                       unsigned char *ok) {
     const int lane = threadIdx.x & 31;
     const unsigned ltmask = (1u << lane) - 1u;
-    auto COL = [&](int i, int t) -> int { return dense ? t : (int)kk[(long long)i * m + t]; };
-    auto CST = [&](int i, int t) -> long long { return (long long)cc[(long long)i * m + t]; };
+    auto COL = [&](int i, int t) -> int { return dense ? t : (int)kk[i * m + t]; };
 
     // 1. column reduction: v_j = min_i c_ij, the first row attaining it owns j.
-    // Rows in order; a row's columns are distinct, so lanes never collide.
-    for (int j = lane; j < n; j += 32) { v[j] = kBigInt; y[j] = -1; }
-    __syncwarp();
-    for (int i = 0; i < n; ++i) {
-        for (int t = lane; t < m; t += 32) {
-            const int j = COL(i, t);
-            const long long c = CST(i, t);
-            if (c < v[j]) { v[j] = c; y[j] = i; }
+    if (dense) {
+        // one lane per column, rows in order
+        for (int j = lane; j < n; j += 32) {
+            long long best = kBigInt;
+            int bi = -1;
+            for (int i = 0; i < n; ++i) {
+                const long long c = cost(i, j, j);
+                if (c < best) { best = c; bi = i; }
+            }
+            v[j] = best;
+            y[j] = bi;
         }
+    } else {
+        // rows in order; a row's columns are distinct, so lanes never collide
+        for (int j = lane; j < n; j += 32) { v[j] = kBigInt; y[j] = -1; }
         __syncwarp();
+        for (int i = 0; i < n; ++i) {
+            for (int t = lane; t < m; t += 32) {
+                const int j = COL(i, t);
+                const long long c = cost(i, t, j);
+                if (c < v[j]) { v[j] = c; y[j] = i; }
+            }
+            __syncwarp();
+        }
     }
+    __syncwarp();
     int bad = 0;
     for (int j = lane; j < n; j += 32)
         if (y[j] < 0) bad = 1;
@@ -104,13 +191,12 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CT *__r
         if (ok[i]) continue;
         long long mn = kBigInt;
         for (int t = lane; t < m; t += 32) {
-            int j = COL(i, t);
+            const int j = COL(i, t);
             if (j == xi) continue;
-            long long h = CST(i, t) - v[j];
+            const long long h = cost(i, t, j) - v[j];
             mn = h < mn ? h : mn;
         }
         mn = wmin_ll(mn);
-        __syncwarp();
         if (lane == 0) v[xi] -= mn;
         __syncwarp();
     }
@@ -128,33 +214,29 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CT *__r
         while (k < l0) {
             if (++guard > gmax) return 9;
             const int i = fr[k++];
-            long long h1 = kLLMax, h2 = kLLMax;
-            int t1 = 0x7fffffff, t2 = 0x7fffffff, cnt = 0;
-            for (int t = lane; t < m; t += 32) {
-                long long h = CST(i, t) - v[COL(i, t)];
-                if (!(h < kBigInt)) continue;   // never enters the two smallest
-                ++cnt;
-                if (h < h1 || (h == h1 && t < t1)) { h2 = h1; t2 = t1; h1 = h; t1 = t; }
-                else if (h < h2 || (h == h2 && t < t2)) { h2 = h; t2 = t; }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                long long oh1 = __shfl_xor_sync(kFull, h1, o), oh2 = __shfl_xor_sync(kFull, h2, o);
-                int ot1 = __shfl_xor_sync(kFull, t1, o), ot2 = __shfl_xor_sync(kFull, t2, o);
-                cnt += __shfl_xor_sync(kFull, cnt, o);
-                bool afirst = (h1 < oh1) || (h1 == oh1 && t1 < ot1);
-                long long fh, sh;
-                int ft, st;
-                if (afirst) {
-                    fh = h1; ft = t1;
-                    bool a2 = (h2 < oh1) || (h2 == oh1 && t2 < ot1);
-                    sh = a2 ? h2 : oh1; st = a2 ? t2 : ot1;
-                } else {
-                    fh = oh1; ft = ot1;
-                    bool b2 = (oh2 < h1) || (oh2 == h1 && ot2 < t1);
-                    sh = b2 ? oh2 : h1; st = b2 ? ot2 : t1;
+            // the two smallest (h, t) of the row with h < BIGINT, and their count
+            unsigned long long k1 = kNoKey, k2 = kNoKey;
+            bool val[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int t = lane + 32 * q;
+                val[q] = false;
+                if (t < m) {
+                    const int j = COL(i, t);
+                    const long long h = cost(i, t, j) - v[j];
+                    if (h < kBigInt) {   // never enters the two smallest
+                        val[q] = true;
+                        const unsigned long long key = ((unsigned long long)(h + kKeyBias) << 6) | (unsigned)t;
+                        if (key < k1) { k2 = k1; k1 = key; }
+                        else if (key < k2) k2 = key;
+                    }
                 }
-                h1 = fh; t1 = ft; h2 = sh; t2 = st;
             }
+            const int cnt = __popc(__ballot_sync(kFull, val[0])) + __popc(__ballot_sync(kFull, val[1]));
+            const unsigned long long m1 = wmin_u64(k1);
+            const unsigned long long m2 = wmin_u64(k1 == m1 ? k2 : k1);   // keys are distinct
+            const int t1 = (int)(m1 & 63u), t2 = (int)(m2 & 63u);
+            const long long h1 = (long long)(m1 >> 6) - kKeyBias, h2 = (long long)(m2 >> 6) - kKeyBias;
             long long u1, u2;
             if (cnt >= 2) { u1 = h1; u2 = h2; j0 = COL(i, t1); j1 = COL(i, t2); }
             else if (cnt == 1) { u1 = h1; u2 = kBigInt; j1 = j0; j0 = COL(i, t1); }
@@ -202,7 +284,7 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CT *__r
             jl[q] = -1;
             if (t < m) {
                 int j = COL(i0, t);
-                long long h = CST(i0, t) - v[j];
+                long long h = cost(i0, t, j) - v[j];
                 dd[j] = h;
                 lab[j] = i0;
                 hl[q] = h;
@@ -249,7 +331,7 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CT *__r
                 if (hm && tpos < 0) tpos = 32 * q + __ffs(hm) - 1;
             }
             if (tpos < 0) return 5;
-            const long long hh = CST(i, tpos) - v[jc] - mn;
+            const long long hh = cost(i, tpos, jc) - v[jc] - mn;
             bool eq[2];
             int jq[2];
             for (int q = 0; q < 2; ++q) {
@@ -260,7 +342,7 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CT *__r
                     int j = COL(i, t);
                     jq[q] = j;
                     if (!ok[j]) {
-                        long long vj = CST(i, t) - hh - v[j];
+                        long long vj = cost(i, t, j) - hh - v[j];
                         if (vj < dd[j]) {
                             dd[j] = vj;
                             lab[j] = i;
@@ -366,12 +448,12 @@ __device__ __forceinline__ DT pdist2(const DT *c1, const DT *c2, int bulk, const
 // The m nearest columns of one row as the binary max-heap of PAIRDISTS
 // (alignutils.f90:641-701): the first m columns are sifted up in order, each
 // later closer column replaces the root and is sifted down.  The heap's array
-// order is the stored order of the row.
-template <typename DT, typename KT>
-__device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, const DT *bi, const DT *acol, int ns, int m,
-                                             int bulk, const double *box) {
+// order is the stored order of the row.  dist(j) is the squared distance to
+// column j.
+template <typename DT, typename KT, typename DF>
+__device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, const DF &dist) {
     for (int j = 0; j < m; ++j) {
-        hd[j] = pdist2<DT>(bi, acol + 3 * j, bulk, box);
+        hd[j] = dist(j);
         hk[j] = (KT)j;
         int l = j + 1;
         while (l > 1) {
@@ -384,7 +466,7 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, const DT *bi, const
         }
     }
     for (int j = m; j < ns; ++j) {
-        DT d = pdist2<DT>(bi, acol + 3 * j, bulk, box);
+        DT d = dist(j);
         if (!(d < hd[0])) continue;
         hd[0] = d;
         hk[0] = (KT)j;
@@ -408,13 +490,93 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, const DT *bi, const
     }
 }
 
+// Coordinates of one permutation group as the assignment sees them: rows are
+// atoms of the fixed structure, columns atoms of the moved one.
+struct GroupCoords {
+    const double *B, *A;     // FP64, 3 per atom
+    const float4 *B4, *A4;   // FP32 copies (mixed form)
+    int bulk;
+    double box[3];
+    float bxf[3];
+};
+
+// Neighbour lists / costs of one group, then its assignment (PAIRDISTS +
+// JOVOSAP for one group).  Returns the assignment's status.
+template <typename KT, typename DT, typename CT, bool RECOMP>
+__device__ int assign_group(const int ns, const int m, const GroupCoords &G, unsigned char *lb,
+                            const RefLayout &L) {
+    const int lane = threadIdx.x & 31;
+    const bool dense = (m == ns);
+    KT *kk = (KT *)(lb + L.lap_kk);
+    long long *v = (long long *)(lb + L.lap_v), *dd = (long long *)(lb + L.lap_d);
+    int *x = (int *)(lb + L.lap_x), *y = (int *)(lb + L.lap_y), *lab = (int *)(lb + L.lap_lab);
+    int *fr = (int *)(lb + L.lap_fr), *todo = (int *)(lb + L.lap_todo);
+    unsigned char *ok = lb + L.lap_ok;
+    if constexpr (RECOMP) {
+        if (!dense) {
+            float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
+            for (int i = lane; i < ns; i += 32) {
+                const float4 bi = G.B4[i];
+                nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return d2_f4(bi, G.A4[j]); });
+            }
+        }
+        __syncwarp();
+        return jv_warp<KT>(ns, m, dense, CostF32<CT>{G.B4, G.A4}, kk, v, dd, x, y, lab, fr, todo, ok);
+    } else {
+        CT *cc = (CT *)(lb + L.lap_cc);
+        constexpr bool kF32 = sizeof(DT) == 4;
+        auto dist = [&](int i, int j) -> DT {
+            if constexpr (kF32)
+                return G.bulk ? d2_f4_box(G.B4[i], G.A4[j], G.bxf) : d2_f4(G.B4[i], G.A4[j]);
+            else
+                return pdist2<double>(G.B + 3 * i, G.A + 3 * j, G.bulk, G.box);
+        };
+        auto cost = [&](DT d) -> CT {
+            if constexpr (kF32) return cost_of_f32<CT>(d);
+            else return (CT)(d * kPScale);
+        };
+        if (dense) {
+            // lanes over columns: conflict-free row stores
+            for (int i = 0; i < ns; ++i)
+                for (int j = lane; j < ns; j += 32) cc[i * m + j] = cost(dist(i, j));
+        } else if constexpr (sizeof(DT) <= sizeof(CT)) {
+            // heap kept in place: distances in the row's cost slots, then
+            // converted from the last slot down (a slot is never overwritten
+            // before it is read)
+            for (int i = lane; i < ns; i += 32) {
+                CT *crow = cc + i * m;
+                DT *hd = reinterpret_cast<DT *>(crow);
+                nearest_heap<DT, KT>(hd, kk + i * m, ns, m, [&](int j) { return dist(i, j); });
+                for (int j = m - 1; j >= 0; --j) crow[j] = cost(hd[j]);
+            }
+        } else {
+            for (int i = lane; i < ns; i += 32) {
+                DT hd[kMaxNei];
+                nearest_heap<DT, KT>(hd, kk + i * m, ns, m, [&](int j) { return dist(i, j); });
+                CT *crow = cc + i * m;
+                for (int j = 0; j < m; ++j) crow[j] = cost(hd[j]);
+            }
+        }
+        __syncwarp();
+        return jv_warp<KT>(ns, m, dense, CostStored<CT>{cc, m}, kk, v, dd, x, y, lab, fr, todo, ok);
+    }
+}
+
+// Resident one-warp blocks per SM the register allocation is sized for
+// (65536 / (32 * FO_REFINE_MINB) registers per thread at most).
+#ifndef FO_REFINE_MINB
+#define FO_REFINE_MINB 16
+#endif
+
 // ---------------------------------------------------------------------------
 // ITERATIVEALIGN from one candidate, executed by one warp (block of 32).
-template <typename DT, typename CT>
-__global__ void __launch_bounds__(32) k_refine_warp(
+template <typename DT, typename CT, bool RECOMP>
+__global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
     const double *xa, const double *xb, const double *peaks, const int *npeaks, unsigned char *lapg,
     double *cdist, double *cR, double *cdisp, double *cxyz, int *cperm, int *cniter, int *cstat) {
+    constexpr bool kF32 = sizeof(DT) == 4;
+    static_assert(kF32 || !RECOMP, "costs are recomputed only from FP32 coordinates");
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double sRb[9], sRn[9], sRc[9];
     const int lane = threadIdx.x;
@@ -430,17 +592,12 @@ __global__ void __launch_bounds__(32) k_refine_warp(
     int maxg = 0;
     for (int gi = 0; gi < P.ngroups; ++gi) maxg = max(maxg, groups[P.group0 + gi].n);
     RefLayout L;
-    ref_layout(n, maxg, sizeof(DT) == 4, (int)sizeof(CT), L);
+    ref_layout(n, maxg, kF32, (int)sizeof(CT), RECOMP, L);
     double *DB = (double *)(smem + L.DB), *A0 = (double *)(smem + L.A0), *DA = (double *)(smem + L.DA);
-    DT *DBf = (DT *)(smem + L.DBf), *DAf = (DT *)(smem + L.DAf);
+    float4 *B4 = (float4 *)(smem + L.DBf), *A4 = (float4 *)(smem + L.DAf);   // mixed form only
     int *permbest = (int *)(smem + L.perm), *newperm = (int *)(smem + L.nperm), *ptmp = (int *)(smem + L.ptmp);
     unsigned char *lb = P.lapstride ? lapg + P.lap0 + (long long)local * P.lapstride : smem + L.coord_end;
-    CT *lcc = (CT *)(lb + L.lap_cc);
-    unsigned short *lkk = (unsigned short *)(lb + L.lap_kk);
-    long long *lv = (long long *)(lb + L.lap_v), *ld = (long long *)(lb + L.lap_d);
-    int *lx = (int *)(lb + L.lap_x), *ly = (int *)(lb + L.lap_y), *llab = (int *)(lb + L.lap_lab);
-    int *lfr = (int *)(lb + L.lap_fr), *ltodo = (int *)(lb + L.lap_todo);
-    unsigned char *lok = lb + L.lap_ok;
+    int *lx = (int *)(lb + L.lap_x);
     const double box[3] = {P.box[0], P.box[1], P.box[2]};
     const double *pk = peaks + 3LL * (P.cand0 + o * P.nrot + ci);
     double d0[3] = {0, 0, 0};
@@ -480,13 +637,17 @@ __global__ void __launch_bounds__(32) k_refine_warp(
     }
     __syncwarp();
     for (int j = lane; j < n; j += 32) {
-        for (int k = 0; k < 3; ++k) {
-            DA[3 * j + k] = A0[3 * j + k];
-            if (sizeof(DT) == 4) { DAf[3 * j + k] = (DT)A0[3 * j + k]; DBf[3 * j + k] = (DT)DB[3 * j + k]; }
+        for (int k = 0; k < 3; ++k) DA[3 * j + k] = A0[3 * j + k];
+        if constexpr (kF32) {
+            A4[j] = make_float4((float)A0[3 * j], (float)A0[3 * j + 1], (float)A0[3 * j + 2], 0.f);
+            B4[j] = make_float4((float)DB[3 * j], (float)DB[3 * j + 1], (float)DB[3 * j + 2], 0.f);
         }
         permbest[j] = j;
     }
     __syncwarp();
+    GroupCoords GC;
+    GC.bulk = bulk;
+    for (int k = 0; k < 3; ++k) { GC.box[k] = box[k]; GC.bxf[k] = (float)box[k]; }
     double db[3] = {0, 0, 0}, newdist = 0;
     int ntries = 0, nperm = n, fail = 0;
     for (int iter = 0; iter < 64 && nperm > 0; ++iter) {
@@ -496,33 +657,12 @@ __global__ void __launch_bounds__(32) k_refine_warp(
         for (int gi = 0; gi < P.ngroups; ++gi) {
             const GroupDev g = groups[P.group0 + gi];
             const int ns = g.n, m = g.m, s0 = g.slot0 - a0;
-            const bool dense = (m == ns);
-            for (int i = lane; i < ns; i += 32) {
-                const DT *bi = DBf + 3 * (s0 + i);
-                CT *crow = lcc + (long long)i * m;
-                if (dense) {
-                    for (int j = 0; j < ns; ++j)
-                        crow[j] = (CT)((double)pdist2<DT>(bi, DAf + 3 * (s0 + j), bulk, box) * kPScale);
-                } else if (sizeof(DT) == 4 && sizeof(CT) == 4) {
-                    // heap kept in place: float distances in the 32-bit cost slots
-                    float *hd = reinterpret_cast<float *>(crow);
-                    unsigned short *hk = lkk + (long long)i * m;
-                    nearest_heap<float, unsigned short>(hd, hk, (const float *)bi, (const float *)DAf + 3 * s0,
-                                                        ns, m, bulk, box);
-                    for (int j = 0; j < m; ++j) crow[j] = (CT)((double)hd[j] * kPScale);
-                } else {
-                    DT hd[kMaxNei];
-                    int hk[kMaxNei];
-                    nearest_heap<DT, int>(hd, hk, bi, DAf + 3 * s0, ns, m, bulk, box);
-                    unsigned short *krow = lkk + (long long)i * m;
-                    for (int j = 0; j < m; ++j) {
-                        crow[j] = (CT)((double)hd[j] * kPScale);
-                        krow[j] = (unsigned short)hk[j];
-                    }
-                }
-            }
-            __syncwarp();
-            int rc = jv_warp<CT>(ns, m, dense, lcc, lkk, lv, ld, lx, ly, llab, lfr, ltodo, lok);
+            GC.B = DB + 3 * s0;
+            GC.A = DA + 3 * s0;
+            GC.B4 = B4 + s0;
+            GC.A4 = A4 + s0;
+            const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP>(ns, m, GC, lb, L)
+                                            : assign_group<uint16_t, DT, CT, RECOMP>(ns, m, GC, lb, L);
             if (rc) fail += 1;
             __syncwarp();
             for (int i = lane; i < ns; i += 32) {
@@ -564,10 +704,9 @@ __global__ void __launch_bounds__(32) k_refine_warp(
             __syncwarp();
             for (int j = lane; j < n; j += 32) {
                 permbest[j] = ptmp[j];
-                for (int k = 0; k < 3; ++k) {
-                    DA[3 * j + k] = A0[3 * ptmp[j] + k] + db[k];
-                    if (sizeof(DT) == 4) DAf[3 * j + k] = (DT)DA[3 * j + k];
-                }
+                for (int k = 0; k < 3; ++k) DA[3 * j + k] = A0[3 * ptmp[j] + k] + db[k];
+                if constexpr (kF32)
+                    A4[j] = make_float4((float)DA[3 * j], (float)DA[3 * j + 1], (float)DA[3 * j + 2], 0.f);
             }
         } else {
             double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -596,10 +735,10 @@ __global__ void __launch_bounds__(32) k_refine_warp(
             for (int j = lane; j < n; j += 32) {
                 permbest[j] = ptmp[j];
                 const double *a = A0 + 3 * ptmp[j];
-                for (int k = 0; k < 3; ++k) {
+                for (int k = 0; k < 3; ++k)
                     DA[3 * j + k] = sRb[3 * k] * a[0] + sRb[3 * k + 1] * a[1] + sRb[3 * k + 2] * a[2];
-                    if (sizeof(DT) == 4) DAf[3 * j + k] = (DT)DA[3 * j + k];
-                }
+                if constexpr (kF32)
+                    A4[j] = make_float4((float)DA[3 * j], (float)DA[3 * j + 1], (float)DA[3 * j + 2], 0.f);
             }
         }
         __syncwarp();
@@ -751,18 +890,20 @@ void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux,
         if (bk.count == 0) continue;
         const int *list = b.cand_list + bk.offset;
         cudaStream_t s = naux ? aux[k % naux] : main;
-#define FO_LAUNCH_REFINE(DT, CT)                                                                   \
-    do {                                                                                          \
-        cudaFuncSetAttribute(k_refine_warp<DT, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                             (int)bk.smem);                                                       \
-        k_refine_warp<DT, CT><<<bk.count, 32, bk.smem, s>>>(                                      \
-            b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,  \
-            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);                                   \
+#define FO_LAUNCH_REFINE(DT, CT, RC)                                                                 \
+    do {                                                                                            \
+        cudaFuncSetAttribute(k_refine_warp<DT, CT, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)bk.smem);                                                         \
+        k_refine_warp<DT, CT, RC><<<bk.count, 32, bk.smem, s>>>(                                    \
+            b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,    \
+            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);                                     \
     } while (0)
-        if (b.fp32) {
-            if (bk.ct64) FO_LAUNCH_REFINE(float, long long); else FO_LAUNCH_REFINE(float, int);
+        if (b.fp32 && b.recomp) {
+            if (bk.ct64) FO_LAUNCH_REFINE(float, long long, true); else FO_LAUNCH_REFINE(float, int, true);
+        } else if (b.fp32) {
+            if (bk.ct64) FO_LAUNCH_REFINE(float, long long, false); else FO_LAUNCH_REFINE(float, int, false);
         } else {
-            if (bk.ct64) FO_LAUNCH_REFINE(double, long long); else FO_LAUNCH_REFINE(double, int);
+            if (bk.ct64) FO_LAUNCH_REFINE(double, long long, false); else FO_LAUNCH_REFINE(double, int, false);
         }
 #undef FO_LAUNCH_REFINE
     }

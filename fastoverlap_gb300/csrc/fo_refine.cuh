@@ -7,21 +7,32 @@ namespace fo {
 
 struct RefLayout {
     size_t DB, A0, DA, DBf, DAf, perm, nperm, ptmp, coord_end;
-    size_t lap_cc, lap_kk, lap_v, lap_d, lap_x, lap_y, lap_lab, lap_fr, lap_todo, lap_ok, lap_end;
+    size_t lap_cc, lap_kk, lap_heap, lap_v, lap_d, lap_x, lap_y, lap_lab, lap_fr, lap_todo, lap_ok, lap_end;
+    int kkbytes;   // bytes per neighbour-list column index
 };
+
+constexpr int kHeapStride = 61;   // floats per lane of the neighbour-heap scratch (odd: no bank conflicts)
 
 __host__ __device__ inline size_t ref_a16(size_t b) { return (b + 15) & ~(size_t)15; }
 
-// n atoms, largest permutation group maxg, FP32 distance copies when fp32,
-// ctsize = bytes per integer cost (4 or 8).
-__host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsize, RefLayout &L) {
+// Column indices of the neighbour lists fit one byte when no group has more
+// than 256 atoms.
+__host__ __device__ inline int ref_kkbytes(int maxg) { return maxg <= 256 ? 1 : 2; }
+
+// n atoms, largest permutation group maxg, FP32 coordinate copies (float4
+// per atom) when fp32, ctsize = bytes per integer cost (4 or 8), recomp =
+// costs recomputed from the FP32 coordinates instead of stored (only the
+// neighbour lists of groups with more than 60 atoms are kept, built through
+// a per-lane heap scratch).
+__host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsize, bool recomp,
+                                           RefLayout &L) {
     size_t o = 0;
     L.DB = o; o += ref_a16(24 * (size_t)n);
     L.A0 = o; o += ref_a16(24 * (size_t)n);
     L.DA = o; o += ref_a16(24 * (size_t)n);
     if (fp32) {
-        L.DBf = o; o += ref_a16(12 * (size_t)n);
-        L.DAf = o; o += ref_a16(12 * (size_t)n);
+        L.DBf = o; o += 16 * (size_t)n;
+        L.DAf = o; o += 16 * (size_t)n;
     } else {
         L.DBf = L.DB;
         L.DAf = L.DA;
@@ -31,9 +42,12 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     L.ptmp = o; o += ref_a16(4 * (size_t)n);
     L.coord_end = o;
     const int m = maxg < 60 ? maxg : 60;
+    const bool sparse = maxg > 60;
+    L.kkbytes = ref_kkbytes(maxg);
     size_t p = 0;
-    L.lap_cc = p; p += ref_a16((size_t)ctsize * maxg * m);
-    L.lap_kk = p; p += (maxg > 60) ? ref_a16(2 * (size_t)maxg * m) : 0;
+    L.lap_cc = p; p += recomp ? 0 : ref_a16((size_t)ctsize * maxg * m);
+    L.lap_kk = p; p += sparse ? ref_a16((size_t)L.kkbytes * maxg * m) : 0;
+    L.lap_heap = p; p += (recomp && sparse) ? ref_a16(4 * 32 * (size_t)kHeapStride) : 0;
     L.lap_v = p; p += ref_a16(8 * (size_t)maxg);
     L.lap_d = p; p += ref_a16(8 * (size_t)maxg);
     L.lap_x = p; p += ref_a16(4 * (size_t)maxg);
