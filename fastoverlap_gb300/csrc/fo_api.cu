@@ -800,8 +800,9 @@ int fo_plan_launches(const fo_plan *pl) {
     int nb = 0;
     for (const auto &b : pl->buckets) nb += b.count > 0;
     // cluster: centre, ylm, radial, coeff, isoft; bulk: prep, sf, 3 fft passes;
-    // then findpeaks, one refinement launch per bucket, select
-    return (pl->bulk ? 5 : 5) + 1 + nb + 1;
+    // then findpeaks (5^3 window, wider windows), one refinement launch per
+    // bucket, select
+    return (pl->bulk ? 5 : 5) + 2 + nb + 1;
 }
 
 void fo_plan_destroy(fo_plan *pl) {
