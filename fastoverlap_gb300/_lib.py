@@ -99,6 +99,7 @@ EXPORTS = {
     "fo_profile_reset": (None, [_vp]),
     "fo_cluster_overlap": (ctypes.c_int, [_vp, _vp, _dp, _dp, _ip, _ip, ctypes.c_int, _dp, _dp]),
     "fo_bulk_overlap": (ctypes.c_int, [_vp, _vp, _dp, _dp, _ip, _ip, ctypes.c_int, _dp]),
+    "fo_findpeaks": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _ip]),
     "fo_bulk_overlap_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _ip, ctypes.c_int,
                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                 ctypes.c_double, ctypes.c_int, ctypes.c_int, _vp,

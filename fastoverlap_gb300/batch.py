@@ -240,6 +240,27 @@ def bulk_overlap(pos1, pos2, box, perm=None, scale=0.0, nwave=0, nfspace=0, prec
     return grid.reshape(M, M, M).transpose(2, 1, 0)
 
 
+def findpeaks(grid, npeaks=10, width=2, precision="fp64", ctx=None):
+    """Peaks of a periodic cubic grid indexed [i1, i2, i3] on the GPU, as the
+    Fortran FINDPEAKS returns them (fastoverlap/f90/fastutils.f90:475-548):
+    (peaks (k, 3) as 1-based fractional grid coordinates, amplitudes (k,)).
+    Raises FoError when no peak is found (where FINDPEAKS stops)."""
+    ctx = ctx or _lib.default_context(precision)
+    g = np.asarray(grid, dtype=np.float64)
+    n = g.shape[0]
+    if g.shape != (n, n, n):
+        raise ValueError("grid must be cubic, got shape %s" % (g.shape,))
+    flat = np.ascontiguousarray(g.transpose(2, 1, 0)).ravel()   # i1 fastest
+    pk = np.zeros(3 * npeaks)
+    am = np.zeros(npeaks)
+    nf = np.zeros(1, np.int32)
+    st = ctx.lib.fo_findpeaks(ctx.h, _lib.d(flat), n, int(npeaks), int(width), _lib.d(pk), _lib.d(am),
+                              _lib.i(nf))
+    ctx.check(st, "findpeaks")
+    k = int(nf[0])
+    return pk[:3 * k].reshape(k, 3), am[:k]
+
+
 def _fastlen(n):
     m = max(1, int(n))
     while True:

@@ -905,6 +905,57 @@ fo_status fo_bulk_overlap(fo_ctx *ctx, const fo_bulk_pair *pair, const double *p
     return s;
 }
 
+fo_status fo_findpeaks(fo_ctx *ctx, const double *grid, int n, int npeaks, int width, double *peaks,
+                       double *amps, int *nfound) {
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    if (!grid || !peaks || !nfound) return set_err(ctx, FO_ERR_BAD_ARGS, "null argument");
+    *nfound = 0;
+    if (n < 2 || n > kMaxM) return set_err(ctx, FO_ERR_BAD_ARGS, "grid side %d outside [2,%d]", n, kMaxM);
+    if (npeaks < 1 || npeaks > kMaxNrot)
+        return set_err(ctx, FO_ERR_BAD_ARGS, "npeaks %d outside [1,%d]", npeaks, kMaxNrot);
+    if (width < 1 || width > 7) return set_err(ctx, FO_ERR_BAD_ARGS, "width %d outside [1,7]", width);
+    cudaSetDevice(ctx->opts.device);
+    const bool fp32 = ctx->opts.precision == FO_PREC_MIXED;
+    const size_t N = (size_t)n * n * n, tsz = fp32 ? 4 : 8;
+    fo::PairDev P{};
+    P.n = 1;
+    P.G = n;
+    P.nrot = npeaks;
+    P.norient = 1;
+    // one allocation: descriptor, grid, overlap max, peaks, amplitudes, counts
+    const size_t o_grid = 256, o_omax = o_grid + ((N * tsz + 255) & ~(size_t)255), o_pk = o_omax + 256,
+                 o_amp = o_pk + ((24 * (size_t)npeaks + 255) & ~(size_t)255),
+                 o_np = o_amp + ((8 * (size_t)npeaks + 255) & ~(size_t)255), total = o_np + 256;
+    unsigned char *d = nullptr;
+    fo_status s = cuda_check(ctx, cudaMalloc(&d, total), "findpeaks allocation");
+    if (s) return s;
+    cudaStream_t st = ctx->stream;
+    std::vector<unsigned char> g(N * tsz);
+    if (fp32)
+        for (size_t i = 0; i < N; ++i) ((float *)g.data())[i] = (float)grid[i];
+    else
+        memcpy(g.data(), grid, N * tsz);
+    cudaMemsetAsync(d, 0, total, st);
+    cudaMemcpyAsync(d, &P, sizeof P, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d + o_grid, g.data(), N * tsz, cudaMemcpyHostToDevice, st);
+    int *d_np = (int *)(d + o_np);
+    fo::launch_findpeaks_from((const fo::PairDev *)d, 1, d + o_grid, (double *)(d + o_omax), (double *)(d + o_pk),
+                              (double *)(d + o_amp), d_np, d_np + 2, fp32, width, st);
+    int cnt[3] = {0, 0, 0};
+    std::vector<double> pk(3 * (size_t)npeaks), am(npeaks);
+    s = cuda_check(ctx, cudaGetLastError(), "findpeaks launch");
+    if (!s) s = cuda_check(ctx, cudaMemcpyAsync(cnt, d_np, sizeof cnt, cudaMemcpyDeviceToHost, st), "copy");
+    if (!s) s = cuda_check(ctx, cudaMemcpyAsync(pk.data(), d + o_pk, 24 * (size_t)npeaks, cudaMemcpyDeviceToHost, st), "copy");
+    if (!s) s = cuda_check(ctx, cudaMemcpyAsync(am.data(), d + o_amp, 8 * (size_t)npeaks, cudaMemcpyDeviceToHost, st), "copy");
+    if (!s) s = cuda_check(ctx, cudaStreamSynchronize(st), "findpeaks");
+    cudaFree(d);
+    if (s) return s;
+    *nfound = cnt[0];
+    memcpy(peaks, pk.data(), 24 * (size_t)cnt[0]);
+    if (amps) memcpy(amps, am.data(), 8 * (size_t)cnt[0]);
+    return cnt[0] > 0 ? FO_OK : set_err(ctx, FO_ERR_NO_PEAKS, "no peak found with half-width up to %d", std::min(n / 2, 7));
+}
+
 // ---------------------------------------------------------------------------
 // Fortran-style entry points
 fo_status fo_setperm(fo_ctx *ctx, int natoms, const int *permgroup, const int *npermsize, int npermgroup) {

@@ -79,6 +79,8 @@ struct RefineBuffers {
     bool recomp;   // costs recomputed from FP32 coordinates (mixed cluster form)
 };
 void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s);
+void launch_findpeaks_from(const PairDev *pairs, int npairs, void *grid, double *omax, double *peaks,
+                           double *amps, int *npeaks, int *pstatus, bool fp32, int width0, cudaStream_t s);
 void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,
                    cudaEvent_t fork, cudaEvent_t *join);
 void launch_select(const RefineBuffers &b, cudaStream_t s);

@@ -379,8 +379,9 @@ __device__ __forceinline__ void lm_start(T (&q)[11], T mx, double mean, int widt
 // written as 1-based fractional grid coordinates (as FINDPEAKS returns
 // them).  A search that finds none leaves npeaks 0 for k_findpeaks_wide.
 template <typename T>
-__global__ void __launch_bounds__(32, FO_PEAKS_MINB) k_findpeaks(const PairDev *pairs, T *grids, double *omax, double *peaks,
-                                                  int *npeaks, double tol) {
+__global__ void __launch_bounds__(32, FO_PEAKS_MINB) k_findpeaks(const PairDev *pairs, T *grids, double *omax,
+                                                                  double *peaks, double *amps, int *npeaks,
+                                                                  double tol) {
     __shared__ T Hg[77];
     constexpr int width = 2, wn = 5;
     const int lane = threadIdx.x, o = blockIdx.x, p = blockIdx.y;
@@ -425,6 +426,7 @@ __global__ void __launch_bounds__(32, FO_PEAKS_MINB) k_findpeaks(const PairDev *
             pk[3 * nfound] = c1;
             pk[3 * nfound + 1] = c2;
             pk[3 * nfound + 2] = c3;
+            if (amps) amps[P.cand0 + o * nrot + nfound] = (double)q[0];
         }
         ++nfound;
         // subtract the fitted peak (not wrapped) and its mean level; the same
@@ -434,11 +436,14 @@ __global__ void __launch_bounds__(32, FO_PEAKS_MINB) k_findpeaks(const PairDev *
     if (lane == 0) npeaks[2 * p + o] = nfound;
 }
 
-// Searches the 5^3 window left without a peak, continued with half-widths
-// 3 .. kMaxWin (while the half-width stays within G/2) on the untouched grid.
+// Searches that found no peak yet (npeaks 0) on the untouched grid, with
+// half-widths width0, width0 + 1, ... while the half-width stays within G/2
+// (the first one unchecked when !check_first, as FINDPEAKS tries its current
+// width before widening) and within kMaxWin.
 template <typename T>
-__global__ void __launch_bounds__(32) k_findpeaks_wide(const PairDev *pairs, T *grids, double *peaks,
-                                                       int *npeaks, int *pstatus, double tol) {
+__global__ void __launch_bounds__(32) k_findpeaks_wide(const PairDev *pairs, T *grids, double *omax,
+                                                       double *peaks, double *amps, int *npeaks, int *pstatus,
+                                                       int width0, int check_first, double tol) {
     __shared__ T Hg[77];
     __shared__ T win[(2 * kMaxWin + 1) * (2 * kMaxWin + 1) * (2 * kMaxWin + 1)];
     const int lane = threadIdx.x, o = blockIdx.x, p = blockIdx.y;
@@ -450,9 +455,11 @@ __global__ void __launch_bounds__(32) k_findpeaks_wide(const PairDev *pairs, T *
     int amax;
     double sum;
     warp_argmax_sum<T>(f, N, mx, amax, sum);
+    if (omax && lane == 0) omax[2 * p + o] = (double)mx;
     int nfound = 0;
     double *pk = peaks + 3LL * (P.cand0 + o * nrot);
-    for (int width = 3; nfound == 0 && width <= G / 2 && width <= kMaxWin; ++width) {
+    for (int width = width0; nfound == 0 && width >= 1 && width <= kMaxWin; ++width) {
+        if ((check_first || width > width0) && width > G / 2) break;
         const int wn = 2 * width + 1;
         for (int np = 0; np < nrot; ++np) {
             const double mean = sum / (double)N;
@@ -476,6 +483,7 @@ __global__ void __launch_bounds__(32) k_findpeaks_wide(const PairDev *pairs, T *
                 pk[3 * nfound] = c1;
                 pk[3 * nfound + 1] = c2;
                 pk[3 * nfound + 2] = c3;
+                if (amps) amps[P.cand0 + o * nrot + nfound] = (double)q[0];
             }
             ++nfound;
             warp_subtract_argmax_sum<T>(f, G, q, c1, c2, c3, mx, amax, sum);
@@ -487,16 +495,31 @@ __global__ void __launch_bounds__(32) k_findpeaks_wide(const PairDev *pairs, T *
     }
 }
 
-void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s) {
-    dim3 grid(2, b.npairs);
+// width0 == 2: the 5^3 kernel, then wider windows from 3 for the grids left
+// without a peak; other starting half-widths go to the wide kernel directly.
+// amps may be null.  npeaks must be zero on entry.
+void launch_findpeaks_from(const PairDev *pairs, int npairs, void *grid, double *omax, double *peaks,
+                           double *amps, int *npeaks, int *pstatus, bool fp32, int width0, cudaStream_t s) {
+    dim3 g(2, npairs);
+    const double tol = fp32 ? 1e-5 : 1e-6;
     if (fp32) {
-        k_findpeaks<float><<<grid, 32, 0, s>>>(b.pairs, (float *)b.grid, b.overlap_max, b.peaks, b.npeaks, 1e-5);
-        k_findpeaks_wide<float><<<grid, 32, 0, s>>>(b.pairs, (float *)b.grid, b.peaks, b.npeaks, b.pstatus, 1e-5);
+        if (width0 == 2)
+            k_findpeaks<float><<<g, 32, 0, s>>>(pairs, (float *)grid, omax, peaks, amps, npeaks, tol);
+        k_findpeaks_wide<float><<<g, 32, 0, s>>>(pairs, (float *)grid, width0 == 2 ? nullptr : omax, peaks,
+                                                 amps, npeaks, pstatus, width0 == 2 ? 3 : width0,
+                                                 width0 == 2 ? 1 : 0, tol);
     } else {
-        k_findpeaks<double><<<grid, 32, 0, s>>>(b.pairs, (double *)b.grid, b.overlap_max, b.peaks, b.npeaks, 1e-6);
-        k_findpeaks_wide<double><<<grid, 32, 0, s>>>(b.pairs, (double *)b.grid, b.peaks, b.npeaks, b.pstatus,
-                                                      1e-6);
+        if (width0 == 2)
+            k_findpeaks<double><<<g, 32, 0, s>>>(pairs, (double *)grid, omax, peaks, amps, npeaks, tol);
+        k_findpeaks_wide<double><<<g, 32, 0, s>>>(pairs, (double *)grid, width0 == 2 ? nullptr : omax, peaks,
+                                                  amps, npeaks, pstatus, width0 == 2 ? 3 : width0,
+                                                  width0 == 2 ? 1 : 0, tol);
     }
+}
+
+void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s) {
+    launch_findpeaks_from(b.pairs, b.npairs, b.grid, b.overlap_max, b.peaks, nullptr, b.npeaks, b.pstatus, fp32,
+                          2, s);
 }
 
 }  // namespace fo

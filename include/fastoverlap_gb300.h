@@ -171,6 +171,20 @@ fo_status fo_bulk_overlap(fo_ctx *ctx, const fo_bulk_pair *pair, const double *p
                           const double *pos2, const int *perm, const int *group_sizes,
                           int index_base, double *grid);
 
+/* ---- peak search on one periodic n^3 grid ----
+ * FINDPEAKS, fastoverlap/f90/fastutils.f90:475-548 (with FINDPEAK :401-444
+ * and FIT :353-397): up to npeaks Gaussian peaks, each fitted in the
+ * (2w+1)^3 window around the current first maximum and subtracted from a
+ * copy of the grid; w starts at `width` (the module variable WIDTH, 2 by
+ * default) and grows while no peak is found, up to min(n/2, 7).  grid: n^3
+ * host doubles, a fastest (left unchanged).  peaks[3k..3k+2]: 1-based
+ * fractional grid coordinates of peak k; amps[k] (may be NULL): its
+ * amplitude X(1).  *nfound: number of peaks.  Mixed precision fits in FP32.
+ * Returns FO_ERR_NO_PEAKS with *nfound = 0 where FINDPEAKS stops.
+ * Limits: 2 <= n <= 256, 1 <= npeaks <= 64, 1 <= width <= 7.               */
+fo_status fo_findpeaks(fo_ctx *ctx, const double *grid, int n, int npeaks, int width,
+                       double *peaks, double *amps, int *nfound);
+
 /* ---- periodic overlap grid without device allocation ----
  * No counterpart in the reference.  For callers that cannot let a library
  * allocate device memory (their own pool owns it, or an allocation in the

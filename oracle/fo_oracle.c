@@ -490,9 +490,17 @@ static int orc_lm_fit(double *p, const double *data, int w, double tol) {
  * ends the search; if nothing was found the window grows by one.          */
 int orc_findpeaks(const double *grid, int n1, int n2, int n3, int npeaks,
                   double *peaks, double *amps) {
+    return orc_findpeaks_w(grid, n1, n2, n3, npeaks, 2, peaks, amps);
+}
+
+/* The same search starting from half-width width0 (FINDPEAKS reads its
+ * width from the module variable WIDTH, :68; the first width is tried
+ * without the MINVAL(FSHAPE)/2 check, later ones with it, :538-544). */
+int orc_findpeaks_w(const double *grid, int n1, int n2, int n3, int npeaks, int width0,
+                    double *peaks, double *amps) {
     const size_t N = (size_t)n1 * n2 * n3;
     double *f = malloc(sizeof(double) * N);
-    int width = 2, nfound = 0;
+    int width = width0, nfound = 0;
     int minshape = n1 < n2 ? n1 : n2;
     if (n3 < minshape) minshape = n3;
     while (nfound == 0) {

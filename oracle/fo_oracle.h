@@ -57,6 +57,8 @@ void   orc_isoft(int bw, const double *ilmm, double *grid_re /* (2bw)^3 */);
 int    orc_findpeaks(const double *grid, int n1, int n2, int n3, int npeaks,
                      double *peaks /* npeaks*3, 1-based fractional */,
                      double *amps);
+int    orc_findpeaks_w(const double *grid, int n1, int n2, int n3, int npeaks, int width0,
+                       double *peaks, double *amps);
 void   orc_eulerm(double a, double b, double g, double R[9]);
 
 /* ---- refinement ---- */

@@ -46,6 +46,7 @@ def lib():
         _LIB.orc_findrotation.restype = ctypes.c_double
         _LIB.orc_iterative_align.restype = ctypes.c_double
         _LIB.orc_findpeaks.restype = ctypes.c_int
+        _LIB.orc_findpeaks_w.restype = ctypes.c_int
         _LIB.orc_jv.restype = ctypes.c_int
         _LIB.orc_cluster_align.restype = ctypes.c_int
         _LIB.orc_bulk_align.restype = ctypes.c_int
@@ -118,13 +119,14 @@ def isoft(ilmm):
     return out.reshape(G, G, G).transpose(2, 1, 0)  # stored alpha fastest
 
 
-def findpeaks(grid, npeaks):
-    """grid indexed [i1, i2, i3]; returns (peaks (np,3) 1-based, amplitudes)."""
+def findpeaks(grid, npeaks, width=2):
+    """grid indexed [i1, i2, i3]; returns (peaks (np,3) 1-based, amplitudes).
+    width: starting window half-width."""
     n1, n2, n3 = grid.shape
     g = np.ascontiguousarray(np.asarray(grid, dtype=np.float64).transpose(2, 1, 0))
     pk = np.zeros(3 * npeaks)
     am = np.zeros(npeaks)
-    nf = lib().orc_findpeaks(_d(g), n1, n2, n3, int(npeaks), _d(pk), _d(am))
+    nf = lib().orc_findpeaks_w(_d(g), n1, n2, n3, int(npeaks), int(width), _d(pk), _d(am))
     if nf < 0:
         raise RuntimeError("no peaks found")
     return pk[:3 * nf].reshape(nf, 3), am[:nf]

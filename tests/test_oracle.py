@@ -149,3 +149,24 @@ def test_parity_check_detects_planted_error(oracle_mod, golden):
     c = oracle_mod.cluster_coeffs(g["A"], g["B"], int(g["L"]), float(g["sigma"]), cutoff=False)
     c[3, 1, 2] += 1e-9 * np.max(np.abs(c))
     assert np.max(np.abs(c - g["coeffs"])) > 1e-12 * np.max(np.abs(g["coeffs"]))
+
+
+@pytest.mark.parametrize("width", [1, 2, 3])
+def test_findpeaks_recovers_planted_gaussians(oracle_mod, width):
+    """Gaussians of the fitted form on a periodic grid: the fitted centres
+    (1-based) are the planted ones, from every starting half-width."""
+    n = 20
+    idx = np.indices((n, n, n)).astype(float)
+    centres = np.array([[4.3, 12.6, 7.1], [15.2, 3.7, 16.4]])
+    f = np.full((n, n, n), 0.25)
+    for k, c in enumerate(centres):
+        d2 = 0.0
+        for a in range(3):
+            d = idx[a] - c[a]
+            d -= n * np.round(d / n)
+            d2 = d2 + d ** 2 / 1.5
+        f += (2.0 - 0.5 * k) * np.exp(-d2)
+    pk, am = oracle_mod.findpeaks(f, 2, width=width)
+    assert pk.shape == (2, 3)
+    np.testing.assert_allclose(pk, centres + 1.0, atol=2e-3)
+    np.testing.assert_allclose(am, [2.0, 1.5], rtol=2e-3)
