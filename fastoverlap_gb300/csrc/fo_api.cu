@@ -57,7 +57,7 @@ struct fo_ctx {
     double prof_ms[kNumKernels] = {0};
     int prof_n[kNumKernels] = {0};
     cudaEvent_t ev[64] = {};
-    static constexpr int kAux = 6;
+    static constexpr int kAux = 16;   // one per refinement footprint class
     cudaStream_t aux[kAux] = {};
     cudaEvent_t fork = nullptr, join[kAux] = {};
     void *flush_buf = nullptr;
@@ -217,12 +217,17 @@ RefAssign ref_assign(int n, int maxg, bool fp32, bool recomp, double dmax) {
     r.ct64 = (dmax * dmax * fo::kPScale >= 2.0e9) ? 1 : 0;
     fo::RefLayout L;
     fo::ref_layout(n, maxg, fp32, r.ct64 ? 8 : 4, recomp, L);
-    // Footprint classes: one launch per class.  Steps of 2 KB up to 16 KB, 4 KB
-    // up to 48 KB and 16 KB beyond keep the rounding (and so the loss of
-    // resident warps per SM) small where most candidates fall.
+    // Footprint classes, one launch each: the largest dynamic shared memory
+    // with which k one-warp blocks stay resident on an SM (233472 bytes per
+    // SM, 1 KB reserved per block, the kernel's static arrays), k = 16 (the
+    // register limit of the kernel) down to 1.  A finer class would not fit
+    // more warps on an SM.
     auto up = [](size_t b) {
-        const size_t step = b <= 16384 ? 2048 : (b <= 49152 ? 4096 : 16384);
-        return (b + step - 1) / step * step;
+        for (int k = 16; k >= 1; --k) {
+            const size_t c = ((size_t)233472 / k - 1024 - 512) & ~(size_t)127;
+            if (b <= c) return c;
+        }
+        return (b + 127) & ~(size_t)127;
     };
     if (L.coord_end + L.lap_end <= kRefSmemCap) {
         r.smem = up(L.coord_end + L.lap_end);
@@ -254,7 +259,10 @@ void build_buckets(fo_plan *pl, const std::vector<RefAssign> &ra, std::vector<in
     }
     pl->buckets.clear();
     cand_list.clear();
-    for (auto &kv : by) {
+    // largest footprint (the heaviest candidates) first: each class has its
+    // own stream, and the longest launches start at once
+    for (auto it = by.rbegin(); it != by.rend(); ++it) {
+        auto &kv = *it;
         // heavier candidates first so the tail of each launch is short
         std::stable_sort(kv.second.begin(), kv.second.end(), [&](int x, int y) {
             return pl->hp[cand2pair_of(pl, x)].n > pl->hp[cand2pair_of(pl, y)].n;

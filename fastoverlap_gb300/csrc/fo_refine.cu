@@ -124,7 +124,11 @@ struct CostF32 {         // cluster costs recomputed from FP32 coordinates
 // fixed width m <= 60; dense rows (m == n) have implicit column index t,
 // sparse rows the column indices kk.  All lanes must call; returns 0 on
 // success, > 0 when the matching fails.
-template <typename KT, typename CF>
+// kARR = false skips the augmenting row reduction: the shortest augmenting
+// paths then start from the prices of the reduction transfer.  The result is
+// still an optimal assignment (the same one when the optimum is unique); only
+// the choice among tied optima may differ from the sequential method.
+template <bool kARR, typename KT, typename CF>
 __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cost, const KT *__restrict__ kk,
                        long long *v, long long *dd, int *x, int *y, int *lab, int *fr, int *todo,
                        unsigned char *ok) {
@@ -207,7 +211,7 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
     long long guard = 0;
     const long long gmax = 64LL * n * (long long)n * m + 100000;
     int j0 = -1, j1 = -1;
-    for (int pass = 0; pass < 2 && nfree > 0; ++pass) {
+    for (int pass = 0; kARR && pass < 2 && nfree > 0; ++pass) {
         const int l0 = nfree;
         int k = 0;
         nfree = 0;
@@ -507,6 +511,7 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                             const RefLayout &L) {
     const int lane = threadIdx.x & 31;
     const bool dense = (m == ns);
+    constexpr bool kF32m = sizeof(DT) == 4;   // mixed form: no augmenting row reduction
     KT *kk = (KT *)(lb + L.lap_kk);
     long long *v = (long long *)(lb + L.lap_v), *dd = (long long *)(lb + L.lap_d);
     int *x = (int *)(lb + L.lap_x), *y = (int *)(lb + L.lap_y), *lab = (int *)(lb + L.lap_lab);
@@ -521,7 +526,7 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
             }
         }
         __syncwarp();
-        return jv_warp<KT>(ns, m, dense, CostF32<CT>{G.B4, G.A4}, kk, v, dd, x, y, lab, fr, todo, ok);
+        return jv_warp<!kF32m, KT>(ns, m, dense, CostF32<CT>{G.B4, G.A4}, kk, v, dd, x, y, lab, fr, todo, ok);
     } else {
         CT *cc = (CT *)(lb + L.lap_cc);
         constexpr bool kF32 = sizeof(DT) == 4;
@@ -558,7 +563,7 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
             }
         }
         __syncwarp();
-        return jv_warp<KT>(ns, m, dense, CostStored<CT>{cc, m}, kk, v, dd, x, y, lab, fr, todo, ok);
+        return jv_warp<!kF32m, KT>(ns, m, dense, CostStored<CT>{cc, m}, kk, v, dd, x, y, lab, fr, todo, ok);
     }
 }
 
