@@ -18,7 +18,7 @@
 
 namespace {
 
-constexpr int kMaxAtoms = 2000;  // refinement keeps 4 coordinate copies in shared memory
+constexpr int kMaxAtoms = 2000;  // refinement keeps two float4 copies + 3 index arrays on chip
 constexpr int kMaxJmax = 31;     // SO(3) grid <= 64^3 (two 64x64 complex slices on chip)
 constexpr int kMaxNrot = 64;
 constexpr int kMaxM = 256;

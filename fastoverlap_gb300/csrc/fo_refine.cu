@@ -497,11 +497,17 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
 // Coordinates of one permutation group as the assignment sees them: rows are
 // atoms of the fixed structure, columns atoms of the moved one.
 struct GroupCoords {
-    const double *B, *A;     // FP64, 3 per atom
+    const double *xb;        // fixed structure as input (3 per atom)
+    double cmb[3];           // its centroid (cluster) or 0 (bulk)
+    const double *A;         // moved structure, FP64 (3 per atom)
     const float4 *B4, *A4;   // FP32 copies (mixed form)
     int bulk;
     double box[3];
     float bxf[3];
+    // fixed-structure atom i as ITERATIVEALIGN holds it (centred for clusters)
+    __device__ __forceinline__ void b(int i, double *o) const {
+        for (int k = 0; k < 3; ++k) o[k] = xb[3 * i + k] - cmb[k];
+    }
 };
 
 // Neighbour lists / costs of one group, then its assignment (PAIRDISTS +
@@ -511,7 +517,7 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                             const RefLayout &L) {
     const int lane = threadIdx.x & 31;
     const bool dense = (m == ns);
-    constexpr bool kF32m = sizeof(DT) == 4;   // mixed form: no augmenting row reduction
+    constexpr bool kF32 = sizeof(DT) == 4;   // mixed form: no augmenting row reduction
     KT *kk = (KT *)(lb + L.lap_kk);
     long long *v = (long long *)(lb + L.lap_v), *dd = (long long *)(lb + L.lap_d);
     int *x = (int *)(lb + L.lap_x), *y = (int *)(lb + L.lap_y), *lab = (int *)(lb + L.lap_lab);
@@ -526,15 +532,15 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
             }
         }
         __syncwarp();
-        return jv_warp<!kF32m, KT>(ns, m, dense, CostF32<CT>{G.B4, G.A4}, kk, v, dd, x, y, lab, fr, todo, ok);
+        return jv_warp<!kF32, KT>(ns, m, dense, CostF32<CT>{G.B4, G.A4}, kk, v, dd, x, y, lab, fr, todo, ok);
     } else {
         CT *cc = (CT *)(lb + L.lap_cc);
-        constexpr bool kF32 = sizeof(DT) == 4;
-        auto dist = [&](int i, int j) -> DT {
+        // squared distance of row i (bi: its FP64 coordinates) and column j
+        auto dist = [&](int i, const double *bi, int j) -> DT {
             if constexpr (kF32)
                 return G.bulk ? d2_f4_box(G.B4[i], G.A4[j], G.bxf) : d2_f4(G.B4[i], G.A4[j]);
             else
-                return pdist2<double>(G.B + 3 * i, G.A + 3 * j, G.bulk, G.box);
+                return pdist2<double>(bi, G.A + 3 * j, G.bulk, G.box);
         };
         auto cost = [&](DT d) -> CT {
             if constexpr (kF32) return cost_of_f32<CT>(d);
@@ -542,28 +548,35 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
         };
         if (dense) {
             // lanes over columns: conflict-free row stores
-            for (int i = 0; i < ns; ++i)
-                for (int j = lane; j < ns; j += 32) cc[i * m + j] = cost(dist(i, j));
+            for (int i = 0; i < ns; ++i) {
+                double bi[3] = {0, 0, 0};
+                if constexpr (!kF32) G.b(i, bi);
+                for (int j = lane; j < ns; j += 32) cc[i * m + j] = cost(dist(i, bi, j));
+            }
         } else if constexpr (sizeof(DT) <= sizeof(CT)) {
             // heap kept in place: distances in the row's cost slots, then
             // converted from the last slot down (a slot is never overwritten
             // before it is read)
             for (int i = lane; i < ns; i += 32) {
+                double bi[3] = {0, 0, 0};
+                if constexpr (!kF32) G.b(i, bi);
                 CT *crow = cc + i * m;
                 DT *hd = reinterpret_cast<DT *>(crow);
-                nearest_heap<DT, KT>(hd, kk + i * m, ns, m, [&](int j) { return dist(i, j); });
+                nearest_heap<DT, KT>(hd, kk + i * m, ns, m, [&](int j) { return dist(i, bi, j); });
                 for (int j = m - 1; j >= 0; --j) crow[j] = cost(hd[j]);
             }
         } else {
             for (int i = lane; i < ns; i += 32) {
+                double bi[3] = {0, 0, 0};
+                if constexpr (!kF32) G.b(i, bi);
                 DT hd[kMaxNei];
-                nearest_heap<DT, KT>(hd, kk + i * m, ns, m, [&](int j) { return dist(i, j); });
+                nearest_heap<DT, KT>(hd, kk + i * m, ns, m, [&](int j) { return dist(i, bi, j); });
                 CT *crow = cc + i * m;
                 for (int j = 0; j < m; ++j) crow[j] = cost(hd[j]);
             }
         }
         __syncwarp();
-        return jv_warp<!kF32m, KT>(ns, m, dense, CostStored<CT>{cc, m}, kk, v, dd, x, y, lab, fr, todo, ok);
+        return jv_warp<!kF32, KT>(ns, m, dense, CostStored<CT>{cc, m}, kk, v, dd, x, y, lab, fr, todo, ok);
     }
 }
 
@@ -575,6 +588,11 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
 
 // ---------------------------------------------------------------------------
 // ITERATIVEALIGN from one candidate, executed by one warp (block of 32).
+// Shared memory holds the FP32 coordinate copies, the permutations and the
+// assignment arrays.  The moved structure's FP64 working coordinates live in
+// the candidate's output slot (cxyz); the fixed structure and the rotated
+// starting structure are recomputed from the inputs where they are read, with
+// the same expressions as when they are first formed.
 template <typename DT, typename CT, bool RECOMP>
 __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
@@ -598,13 +616,15 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     for (int gi = 0; gi < P.ngroups; ++gi) maxg = max(maxg, groups[P.group0 + gi].n);
     RefLayout L;
     ref_layout(n, maxg, kF32, (int)sizeof(CT), RECOMP, L);
-    double *DB = (double *)(smem + L.DB), *A0 = (double *)(smem + L.A0), *DA = (double *)(smem + L.DA);
     float4 *B4 = (float4 *)(smem + L.DBf), *A4 = (float4 *)(smem + L.DAf);   // mixed form only
     int *permbest = (int *)(smem + L.perm), *newperm = (int *)(smem + L.nperm), *ptmp = (int *)(smem + L.ptmp);
     unsigned char *lb = P.lapstride ? lapg + P.lap0 + (long long)local * P.lapstride : smem + L.coord_end;
     int *lx = (int *)(lb + L.lap_x);
     const double box[3] = {P.box[0], P.box[1], P.box[2]};
     const double *pk = peaks + 3LL * (P.cand0 + o * P.nrot + ci);
+    const long long ob = P.candatom0 + (long long)local * n;
+    double *DA = cxyz + 3 * ob;                            // moved structure, FP64
+    const double *XA = xa + 3LL * a0, *XB = xb + 3LL * a0;   // inputs of the pair
     double d0[3] = {0, 0, 0};
     if (lane == 0) {
         for (int k = 0; k < 9; ++k) { sRb[k] = (k % 4 == 0) ? 1.0 : 0.0; sRc[k] = sRb[k]; }
@@ -617,42 +637,54 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
         for (int k = 0; k < 3; ++k) d0[k] = (pk[k] - 1.0) * box[k] / P.G;
     __syncwarp();
     const double sgn = (o == 1) ? -1.0 : 1.0;
-    double cs[6] = {0, 0, 0, 0, 0, 0};
-    for (int j = lane; j < n; j += 32) {
-        const double *a = xa + 3LL * (a0 + j), *b = xb + 3LL * (a0 + j);
-        for (int k = 0; k < 3; ++k) DB[3 * j + k] = b[k];
+    // moved atom j rotated by the candidate (cluster) or shifted (bulk)
+    auto a_raw = [&](int j, double *out) {
+        const double *a = XA + 3 * j;
         if (bulk) {
-            for (int k = 0; k < 3; ++k) A0[3 * j + k] = a[k] - d0[k];
+            for (int k = 0; k < 3; ++k) out[k] = a[k] - d0[k];
         } else {
             for (int k = 0; k < 3; ++k)
-                A0[3 * j + k] = sgn * (sRc[3 * k] * a[0] + sRc[3 * k + 1] * a[1] + sRc[3 * k + 2] * a[2]);
+                out[k] = sgn * (sRc[3 * k] * a[0] + sRc[3 * k + 1] * a[1] + sRc[3 * k + 2] * a[2]);
         }
-        for (int k = 0; k < 3; ++k) { cs[k] += A0[3 * j + k]; cs[3 + k] += DB[3 * j + k]; }
+    };
+    double cs[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = lane; j < n; j += 32) {
+        double t[3];
+        a_raw(j, t);
+        for (int k = 0; k < 3; ++k) { cs[k] += t[k]; cs[3 + k] += XB[3 * j + k]; }
     }
     for (int k = 0; k < 6; ++k) cs[k] = wsum_d(cs[k]);
-    double cmb[3] = {0, 0, 0};
-    __syncwarp();
-    if (!bulk) {  // ITERATIVEALIGN works on structures centred at their centroids
-        for (int k = 0; k < 3; ++k) cmb[k] = cs[3 + k] / n;
-        for (int j = lane; j < n; j += 32)
-            for (int k = 0; k < 3; ++k) {
-                A0[3 * j + k] -= cs[k] / n;
-                DB[3 * j + k] -= cmb[k];
-            }
+    // ITERATIVEALIGN works on structures centred at their centroids
+    double ca[3] = {0, 0, 0};
+    GroupCoords GC;
+    GC.bulk = bulk;
+    for (int k = 0; k < 3; ++k) {
+        GC.cmb[k] = bulk ? 0.0 : cs[3 + k] / n;
+        ca[k] = cs[k] / n;
+        GC.box[k] = box[k];
+        GC.bxf[k] = (float)box[k];
     }
-    __syncwarp();
+    // starting moved structure A0 (centred for clusters)
+    auto a_start = [&](int j, double *out) {
+        a_raw(j, out);
+        if (!bulk)
+            for (int k = 0; k < 3; ++k) out[k] -= ca[k];
+    };
+    GC.xb = XB;
     for (int j = lane; j < n; j += 32) {
-        for (int k = 0; k < 3; ++k) DA[3 * j + k] = A0[3 * j + k];
+        double a[3];
+        a_start(j, a);
+        for (int k = 0; k < 3; ++k) DA[3 * j + k] = a[k];
         if constexpr (kF32) {
-            A4[j] = make_float4((float)A0[3 * j], (float)A0[3 * j + 1], (float)A0[3 * j + 2], 0.f);
-            B4[j] = make_float4((float)DB[3 * j], (float)DB[3 * j + 1], (float)DB[3 * j + 2], 0.f);
+            double b[3];
+            GC.b(j, b);
+            A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
+            B4[j] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.f);
         }
         permbest[j] = j;
     }
     __syncwarp();
-    GroupCoords GC;
-    GC.bulk = bulk;
-    for (int k = 0; k < 3; ++k) { GC.box[k] = box[k]; GC.bxf[k] = (float)box[k]; }
+    const GroupCoords GB = GC;   // whole-structure view of the fixed structure
     double db[3] = {0, 0, 0}, newdist = 0;
     int ntries = 0, nperm = n, fail = 0;
     for (int iter = 0; iter < 64 && nperm > 0; ++iter) {
@@ -662,7 +694,7 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
         for (int gi = 0; gi < P.ngroups; ++gi) {
             const GroupDev g = groups[P.group0 + gi];
             const int ns = g.n, m = g.m, s0 = g.slot0 - a0;
-            GC.B = DB + 3 * s0;
+            GC.xb = XB + 3 * s0;
             GC.A = DA + 3 * s0;
             GC.B4 = B4 + s0;
             GC.A4 = A4 + s0;
@@ -675,7 +707,9 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
                 if (col >= ns) { col = ns - 1; fail += 1; }
                 if (col < 0) { col = 0; fail += 1; }
                 newperm[s0 + i] = s0 + col;
-                pdsum += pdist2<double>(DB + 3 * (s0 + i), DA + 3 * (s0 + col), bulk, box);
+                double b[3];
+                GC.b(i, b);
+                pdsum += pdist2<double>(b, DA + 3 * (s0 + col), bulk, box);
             }
             __syncwarp();
         }
@@ -691,8 +725,10 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
             double s3[3] = {0, 0, 0};
             for (int j = lane; j < n; j += 32) {
                 const double *a = DA + 3 * newperm[j];
+                double b[3];
+                GB.b(j, b);
                 for (int k = 0; k < 3; ++k) {
-                    double t = DB[3 * j + k] - a[k];
+                    double t = b[k] - a[k];
                     s3[k] += t - box[k] * round(t / box[k]);
                 }
             }
@@ -701,22 +737,27 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
             double s1 = 0;
             for (int j = lane; j < n; j += 32) {
                 const double *a = DA + 3 * newperm[j];
-                double ad[3] = {a[0] + dn[0], a[1] + dn[1], a[2] + dn[2]};
-                s1 += pdist2<double>(DB + 3 * j, ad, 1, box);
+                double ad[3] = {a[0] + dn[0], a[1] + dn[1], a[2] + dn[2]}, b[3];
+                GB.b(j, b);
+                s1 += pdist2<double>(b, ad, 1, box);
             }
             newdist = sqrt(wsum_d(s1));
             for (int k = 0; k < 3; ++k) db[k] += dn[k];
             __syncwarp();
             for (int j = lane; j < n; j += 32) {
                 permbest[j] = ptmp[j];
-                for (int k = 0; k < 3; ++k) DA[3 * j + k] = A0[3 * ptmp[j] + k] + db[k];
+                double a[3];
+                a_start(ptmp[j], a);
+                for (int k = 0; k < 3; ++k) DA[3 * j + k] = a[k] + db[k];
                 if constexpr (kF32)
                     A4[j] = make_float4((float)DA[3 * j], (float)DA[3 * j + 1], (float)DA[3 * j + 2], 0.f);
             }
         } else {
             double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
             for (int j = lane; j < n; j += 32) {
-                const double *b = DB + 3 * j, *a = DA + 3 * newperm[j];
+                const double *a = DA + 3 * newperm[j];
+                double b[3];
+                GB.b(j, b);
                 double xm = b[0] - a[0], ym = b[1] - a[1], zm = b[2] - a[2];
                 double xp = b[0] + a[0], yp = b[1] + a[1], zp = b[2] + a[2];
                 q[0] += xm * xm + ym * ym + zm * zm;
@@ -739,7 +780,8 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
             __syncwarp();
             for (int j = lane; j < n; j += 32) {
                 permbest[j] = ptmp[j];
-                const double *a = A0 + 3 * ptmp[j];
+                double a[3];
+                a_start(ptmp[j], a);
                 for (int k = 0; k < 3; ++k)
                     DA[3 * j + k] = sRb[3 * k] * a[0] + sRb[3 * k + 1] * a[1] + sRb[3 * k + 2] * a[2];
                 if constexpr (kF32)
@@ -756,17 +798,21 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     // final minimisation without a new permutation
     if (bulk) {
         double s3[3] = {0, 0, 0};
-        for (int j = lane; j < n; j += 32)
+        for (int j = lane; j < n; j += 32) {
+            double b[3];
+            GB.b(j, b);
             for (int k = 0; k < 3; ++k) {
-                double t = DB[3 * j + k] - DA[3 * j + k];
+                double t = b[k] - DA[3 * j + k];
                 s3[k] += t - box[k] * round(t / box[k]);
             }
+        }
         double dn[3];
         for (int k = 0; k < 3; ++k) dn[k] = wsum_d(s3[k]) / n;
         double s1 = 0;
         for (int j = lane; j < n; j += 32) {
-            double ad[3] = {DA[3 * j] + dn[0], DA[3 * j + 1] + dn[1], DA[3 * j + 2] + dn[2]};
-            s1 += pdist2<double>(DB + 3 * j, ad, 1, box);
+            double ad[3] = {DA[3 * j] + dn[0], DA[3 * j + 1] + dn[1], DA[3 * j + 2] + dn[2]}, b[3];
+            GB.b(j, b);
+            s1 += pdist2<double>(b, ad, 1, box);
         }
         newdist = sqrt(wsum_d(s1));
         for (int k = 0; k < 3; ++k) db[k] += dn[k];
@@ -776,7 +822,9 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     } else {
         double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         for (int j = lane; j < n; j += 32) {
-            const double *b = DB + 3 * j, *a = DA + 3 * j;
+            const double *a = DA + 3 * j;
+            double b[3];
+            GB.b(j, b);
             double xm = b[0] - a[0], ym = b[1] - a[1], zm = b[2] - a[2];
             double xp = b[0] + a[0], yp = b[1] + a[1], zp = b[2] + a[2];
             q[0] += xm * xm + ym * ym + zm * zm;
@@ -800,15 +848,11 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
         for (int j = lane; j < n; j += 32) {
             double a[3] = {DA[3 * j], DA[3 * j + 1], DA[3 * j + 2]};
             for (int k = 0; k < 3; ++k)
-                DA[3 * j + k] = sRn[3 * k] * a[0] + sRn[3 * k + 1] * a[1] + sRn[3 * k + 2] * a[2] + cmb[k];
+                DA[3 * j + k] = sRn[3 * k] * a[0] + sRn[3 * k + 1] * a[1] + sRn[3 * k + 2] * a[2] + GB.cmb[k];
         }
     }
     __syncwarp();
-    const long long ob = P.candatom0 + (long long)local * n;
-    for (int j = lane; j < n; j += 32) {
-        cperm[ob + j] = permbest[j];
-        for (int k = 0; k < 3; ++k) cxyz[3 * (ob + j) + k] = DA[3 * j + k];
-    }
+    for (int j = lane; j < n; j += 32) cperm[ob + j] = permbest[j];
     for (int o2 = 16; o2 > 0; o2 >>= 1) fail += __shfl_xor_sync(kFull, fail, o2);
     if (lane == 0) {
         cdist[c] = newdist;

@@ -6,7 +6,7 @@
 namespace fo {
 
 struct RefLayout {
-    size_t DB, A0, DA, DBf, DAf, perm, nperm, ptmp, coord_end;
+    size_t DBf, DAf, perm, nperm, ptmp, coord_end;
     size_t lap_cc, lap_kk, lap_heap, lap_v, lap_d, lap_x, lap_y, lap_lab, lap_fr, lap_todo, lap_ok, lap_end;
     int kkbytes;   // bytes per neighbour-list column index
 };
@@ -23,20 +23,13 @@ __host__ __device__ inline int ref_kkbytes(int maxg) { return maxg <= 256 ? 1 : 
 // per atom) when fp32, ctsize = bytes per integer cost (4 or 8), recomp =
 // costs recomputed from the FP32 coordinates instead of stored (only the
 // neighbour lists of groups with more than 60 atoms are kept, built through
-// a per-lane heap scratch).
+// a per-lane heap scratch).  The FP64 coordinates are not held here: the
+// refinement keeps them in global memory.
 __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsize, bool recomp,
                                            RefLayout &L) {
     size_t o = 0;
-    L.DB = o; o += ref_a16(24 * (size_t)n);
-    L.A0 = o; o += ref_a16(24 * (size_t)n);
-    L.DA = o; o += ref_a16(24 * (size_t)n);
-    if (fp32) {
-        L.DBf = o; o += 16 * (size_t)n;
-        L.DAf = o; o += 16 * (size_t)n;
-    } else {
-        L.DBf = L.DB;
-        L.DAf = L.DA;
-    }
+    L.DBf = o; o += fp32 ? 16 * (size_t)n : 0;
+    L.DAf = o; o += fp32 ? 16 * (size_t)n : 0;
     L.perm = o; o += ref_a16(4 * (size_t)n);
     L.nperm = o; o += ref_a16(4 * (size_t)n);
     L.ptmp = o; o += ref_a16(4 * (size_t)n);
@@ -47,7 +40,6 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     size_t p = 0;
     L.lap_cc = p; p += recomp ? 0 : ref_a16((size_t)ctsize * maxg * m);
     L.lap_kk = p; p += sparse ? ref_a16((size_t)L.kkbytes * maxg * m) : 0;
-    L.lap_heap = p; p += (recomp && sparse) ? ref_a16(4 * 32 * (size_t)kHeapStride) : 0;
     L.lap_v = p; p += ref_a16(8 * (size_t)maxg);
     L.lap_d = p; p += ref_a16(8 * (size_t)maxg);
     L.lap_x = p; p += ref_a16(4 * (size_t)maxg);
@@ -56,7 +48,11 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     L.lap_fr = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_todo = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_ok = p; p += ref_a16((size_t)maxg);
-    L.lap_end = p;
+    // the neighbour-heap scratch is only used before a group's assignment
+    // starts, so it overlays the assignment arrays
+    L.lap_heap = L.lap_v;
+    const size_t heap_end = L.lap_v + ((recomp && sparse) ? ref_a16(4 * 32 * (size_t)kHeapStride) : 0);
+    L.lap_end = p > heap_end ? p : heap_end;
 }
 
 }  // namespace fo
