@@ -356,6 +356,8 @@ fo_status fo_ctx_create(const fo_opts *opts, fo_ctx **out) {
         delete c;
         return FO_ERR_CUDA;
     }
+    fo::init_sph_tables();   // constant tables of this device (idempotent)
+    if (cudaGetLastError() != cudaSuccess) { delete c; return FO_ERR_CUDA; }
     *out = c;
     return FO_OK;
 }

@@ -61,6 +61,13 @@ template <typename T> struct cplx;
 template <> struct cplx<double> { using type = double2; };
 template <> struct cplx<float> { using type = float2; };
 
+// a complex value from two parts of the element type itself (no FP64 detour)
+template <typename T2, typename S> __host__ __device__ inline T2 pack2(S a, S b) {
+    T2 r;
+    r.x = a;
+    r.y = b;
+    return r;
+}
 template <typename T2> __host__ __device__ inline T2 mk2(double a, double b) {
     T2 r; r.x = a; r.y = b; return r;
 }
@@ -116,12 +123,44 @@ __host__ __device__ inline int fft_factor(int n, int *rad) {
     return k;
 }
 
+// twiddle exp(sign 2 pi i e/n) for 0 <= e < n
 template <typename T2>
-__device__ inline T2 tw_get(const T2 *tw, int n, long long e, int sign) {
-    int t = (int)(((e % n) + n) % n);
-    T2 w = tw[t];
+__device__ __forceinline__ T2 tw_at(const T2 *tw, int e, int sign) {
+    T2 w = tw[e];
     if (sign < 0) w.y = -w.y;
     return w;
+}
+
+// One radix-P Stockham pass over all lines (Ns: product of the earlier
+// radices).  The twiddle index k r n/(Ns P) of the inputs stays below n, and
+// the butterfly's own twiddles W_P^{rq} are tw[((r q) mod P) n/P] with the
+// exponent reduced at compile time.
+template <int P, typename T2>
+__device__ __forceinline__ void fft_pass(const T2 *x, T2 *y, int n, int nlines, int lstride, int estride,
+                                         int sign, const T2 *tw, int Ns) {
+    const int nb = n / P, tstep = n / (Ns * P);
+    for (int t = threadIdx.x; t < nlines * nb; t += blockDim.x) {
+        const int l = t / nb, j = t % nb, k = j % Ns;
+        const T2 *xl = x + (long long)l * lstride;
+        T2 *yl = y + (long long)l * lstride;
+        T2 v[P];
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+            const T2 a = xl[(long long)(j + r * nb) * estride];
+            v[r] = (r == 0 || k == 0) ? a : cmul(a, tw_at(tw, k * r * tstep, sign));
+        }
+        const int idxD = (j / Ns) * Ns * P + k;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            T2 acc = v[0];
+#pragma unroll
+            for (int r = 1; r < P; ++r) {
+                const int m = (r * q) % P;
+                acc = cadd(acc, m == 0 ? v[r] : cmul(v[r], tw_at(tw, m * nb, sign)));
+            }
+            yl[(long long)(idxD + q * Ns) * estride] = acc;
+        }
+    }
 }
 
 template <typename T2>
@@ -129,13 +168,13 @@ __device__ T2 *fft_lines(T2 *x, T2 *y, int n, int nlines, int lstride, int estri
                          const T2 *tw) {
     int rad[24];
     int nr = fft_factor(n, rad);
-    if (nr < 0) {  // direct DFT
+    if (nr < 0) {  // direct DFT (n <= 256, so j q < 2^31)
         for (int t = threadIdx.x; t < nlines * n; t += blockDim.x) {
             int l = t / n, q = t % n;
             const T2 *xl = x + (long long)l * lstride;
             T2 acc = mk2<T2>(0, 0);
             for (int j = 0; j < n; ++j)
-                acc = cadd(acc, cmul(xl[(long long)j * estride], tw_get(tw, n, (long long)j * q, sign)));
+                acc = cadd(acc, cmul(xl[(long long)j * estride], tw_at(tw, (j * q) % n, sign)));
             y[(long long)l * lstride + (long long)q * estride] = acc;
         }
         __syncthreads();
@@ -143,24 +182,12 @@ __device__ T2 *fft_lines(T2 *x, T2 *y, int n, int nlines, int lstride, int estri
     }
     int Ns = 1;
     for (int s = 0; s < nr; ++s) {
-        const int p = rad[s], nb = n / p, tstep = n / (Ns * p);
-        for (int t = threadIdx.x; t < nlines * nb; t += blockDim.x) {
-            int l = t / nb, j = t % nb, k = j % Ns;
-            const T2 *xl = x + (long long)l * lstride;
-            T2 *yl = y + (long long)l * lstride;
-            T2 v[5], o[5];
-            for (int r = 0; r < p; ++r) {
-                T2 a = xl[(long long)(j + r * nb) * estride];
-                v[r] = (r == 0 || k == 0) ? a : cmul(a, tw_get(tw, n, (long long)k * r * tstep, sign));
-            }
-            for (int q = 0; q < p; ++q) {
-                T2 acc = v[0];
-                for (int r = 1; r < p; ++r)
-                    acc = cadd(acc, cmul(v[r], tw_get(tw, n, (long long)r * q * (n / p), sign)));
-                o[q] = acc;
-            }
-            int idxD = (j / Ns) * Ns * p + k;
-            for (int q = 0; q < p; ++q) yl[(long long)(idxD + q * Ns) * estride] = o[q];
+        const int p = rad[s];
+        switch (p) {
+            case 4: fft_pass<4, T2>(x, y, n, nlines, lstride, estride, sign, tw, Ns); break;
+            case 2: fft_pass<2, T2>(x, y, n, nlines, lstride, estride, sign, tw, Ns); break;
+            case 3: fft_pass<3, T2>(x, y, n, nlines, lstride, estride, sign, tw, Ns); break;
+            default: fft_pass<5, T2>(x, y, n, nlines, lstride, estride, sign, tw, Ns); break;
         }
         __syncthreads();
         T2 *tmp = x; x = y; y = tmp;

@@ -19,12 +19,13 @@ struct SphBuffers {
     void *W;                // radial weights (T)
     void *coef;             // complex T coefficients (ilmm layout)
     void *grid;             // real T overlap grids
-    const void *const *dtab;  // per bandwidth: Wigner table (T), layout [k][m1][m2][l]
+    const void *const *dtab;  // per bandwidth: Wigner table (T), layout [k][l][m1][m2]
     int npairs, ngroups, nslots, maxL, maxG, maxgroup;
 };
 
 // spherical stages
 void launch_sph_center(const SphBuffers &b, cudaStream_t s);
+void init_sph_tables();   // constant tables of the current device; before the first launch
 void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s);
 void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s);
 void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s);

@@ -60,48 +60,97 @@ __global__ void k_sph_center(PairDev *pairs, const int *slot2orig, const double 
 }
 
 // ---------------------------------------------------------------------------
+// Recurrence factors of the orthonormal associated Legendre functions, for
+// l, m < kYlmMax (Jmax <= 31), in FP64 and FP32:
+//   a[l][m] = sqrt((4l^2 - 1) / (l^2 - m^2))            (l >= m + 2)
+//   b[l][m] = sqrt(((l-1)^2 - m^2) / (4(l-1)^2 - 1))     (l >= m + 2)
+//   c[m] = sqrt(2m + 3)  (l = m + 1),   d[m] = sqrt((2m + 1) / 2m)  (m >= 1)
+// Numerators and denominators are exact integers and the quotient and root
+// are correctly rounded on host and device alike, so the table holds the
+// values a direct FP64 evaluation gives.
+constexpr int kYlmMax = 32;
+constexpr int kYlmTab = 2 * kYlmMax * kYlmMax + 2 * kYlmMax;
+__constant__ double c_ylm64[kYlmTab];
+__constant__ float c_ylm32[kYlmTab];
+
+void init_sph_tables() {
+    double t64[kYlmTab] = {0};
+    float t32[kYlmTab];
+    for (int l = 0; l < kYlmMax; ++l)
+        for (int m = 0; m + 2 <= l; ++m) {
+            t64[l * kYlmMax + m] = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+            t64[kYlmMax * kYlmMax + l * kYlmMax + m] =
+                sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+        }
+    for (int m = 0; m < kYlmMax; ++m) {
+        t64[2 * kYlmMax * kYlmMax + m] = sqrt(2.0 * m + 3.0);
+        t64[2 * kYlmMax * kYlmMax + kYlmMax + m] = m > 0 ? sqrt((2.0 * m + 1.0) / (2.0 * m)) : 0.0;
+    }
+    for (int q = 0; q < kYlmTab; ++q) t32[q] = (float)t64[q];
+    cudaMemcpyToSymbol(c_ylm64, t64, sizeof t64);
+    cudaMemcpyToSymbol(c_ylm32, t32, sizeof t32);
+}
+
+template <typename T> __device__ __forceinline__ const T *ylm_tab();
+template <> __device__ __forceinline__ const double *ylm_tab<double>() { return c_ylm64; }
+template <> __device__ __forceinline__ const float *ylm_tab<float>() { return c_ylm32; }
+
 // Orthonormal Y_lm (Condon-Shortley phase) for l <= L of every slot of both
-// structures; one thread per (slot, side).  Output per slot: (L+1)^2 complex
-// values at index l*l + l + m.  An atom at the origin gets theta = 0.
-template <typename T2>
+// structures; one thread per (slot, side), computed in the precision T of the
+// output.  Output per slot: (L+1)^2 complex values at index l*l + l + m.  An
+// atom at the origin gets theta = 0.  FP64: e^{i m phi} from sincos(m phi);
+// FP32: by repeated multiplication with e^{i phi}.
+template <typename T, typename T2>
 __global__ void k_sph_ylm(const PairDev *pairs, const int *slot2pair, const double *xa,
                           const double *xb, double *ra, double *rb, T2 *ylmA, T2 *ylmB,
                           int nslots) {
+    constexpr bool kF32 = sizeof(T) == 4;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 2 * nslots) return;
     const int side = t / nslots, slot = t % nslots;
     const PairDev &P = pairs[slot2pair[slot]];
     const int L = P.L;
     const double *X = side ? xb : xa;
-    double x = X[3 * slot], y = X[3 * slot + 1], z = X[3 * slot + 2];
-    double r = sqrt(x * x + y * y + z * z);
-    double ct = 1.0, phi = 0.0;
-    if (r > 0.0) {
-        ct = fmin(1.0, fmax(-1.0, z / r));
-        phi = atan2(y, x);
-    }
-    double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    const double x = X[3 * slot], y = X[3 * slot + 1], z = X[3 * slot + 2];
+    const double r = sqrt(x * x + y * y + z * z);
     (side ? rb : ra)[slot] = r;
+    const T *A = ylm_tab<T>(), *B = A + kYlmMax * kYlmMax, *C = B + kYlmMax * kYlmMax, *D = C + kYlmMax;
+    T ct = 1, cph = 1, sph = 0;
+    double phi = 0.0;
+    if (r > 0.0) {
+        if constexpr (kF32) {
+            const float xf = (float)x, yf = (float)y, rho = sqrtf(xf * xf + yf * yf);
+            ct = fminf(1.f, fmaxf(-1.f, (float)z / (float)r));
+            if (rho > 0.f) { cph = xf / rho; sph = yf / rho; }
+        } else {
+            ct = fmin(1.0, fmax(-1.0, z / r));
+            phi = atan2(y, x);
+        }
+    }
+    const T st = sqrt(ct * ct < T(1) ? T(1) - ct * ct : T(0));
     T2 *out = (side ? ylmB : ylmA) + P.ylm0 + (long long)(slot - P.atom0) * (L + 1) * (L + 1);
-    double pmm = 0.28209479177387814347;  // 1/sqrt(4 pi)
+    T pmm = T(0.28209479177387814347);  // 1/sqrt(4 pi)
+    T cm = 1, sm = 0;
     for (int m = 0; m <= L; ++m) {
-        if (m > 0) pmm = -sqrt((2.0 * m + 1.0) / (2.0 * m)) * st * pmm;
-        double sm, cm;
-        sincos(m * phi, &sm, &cm);
-        double sgn = (m & 1) ? -1.0 : 1.0;
-        double p2 = 0.0, p1 = pmm;
-        for (int l = m; l <= L; ++l) {
-            double pl;
-            if (l == m) pl = pmm;
-            else if (l == m + 1) pl = sqrt(2.0 * m + 3.0) * ct * pmm;
-            else {
-                double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
-                double b = sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
-                pl = a * (ct * p1 - b * p2);
+        if (m > 0) {
+            pmm = -D[m] * st * pmm;
+            if constexpr (kF32) {
+                const T c2 = cm * cph - sm * sph;
+                sm = sm * cph + cm * sph;
+                cm = c2;
             }
+        }
+        if constexpr (!kF32) sincos(m * phi, &sm, &cm);
+        const T sgn = (m & 1) ? T(-1) : T(1);
+        T p2 = 0, p1 = pmm;
+        for (int l = m; l <= L; ++l) {
+            T pl;
+            if (l == m) pl = pmm;
+            else if (l == m + 1) pl = C[m] * ct * pmm;
+            else pl = A[l * kYlmMax + m] * (ct * p1 - B[l * kYlmMax + m] * p2);
             if (l > m) { p2 = p1; p1 = pl; }
-            out[l * l + l + m] = mk2<T2>(pl * cm, pl * sm);
-            if (m > 0) out[l * l + l - m] = mk2<T2>(sgn * pl * cm, -sgn * pl * sm);
+            out[l * l + l + m] = pack2<T2, T>(pl * cm, pl * sm);
+            if (m > 0) out[l * l + l - m] = pack2<T2, T>(sgn * pl * cm, -sgn * pl * sm);
         }
     }
 }
@@ -113,11 +162,16 @@ __global__ void k_sph_ylm(const PairDev *pairs, const int *slot2pair, const doub
 // nothing overflows.  e^{-x} i_l(x) comes from Miller's backward recurrence
 // i_{l-1} = i_{l+1} + (2l+1)/x i_l started at l = L + 10 + 0.8x (full FP64
 // accuracy for L <= 63) and normalised by e^{-x} i_0 = (1 - e^{-2x})/2x; for
-// x < 1e-6 the leading series terms are used.  Layout per group:
-// W[w0 + (l*n + b)*n + a].
+// x < 1e-6 the leading series terms are used.  Evaluated in the precision T of
+// the weights (the recurrence is rescaled before it can overflow T: by 1e-250
+// above 1e250 in FP64, by 1e-28 above 1e28 in FP32, which leaves room for a
+// step's growth (2k+1)/x < 1e8 at x >= 1e-6).  The cutoff test is made in
+// FP64 in both precisions.  Layout per group: W[w0 + (l*n + b)*n + a].
 template <typename T>
 __global__ void k_sph_radial(const PairDev *pairs, const GroupDev *groups, const double *ra,
                              const double *rb, T *W, int cutoff) {
+    constexpr T kBig = sizeof(T) == 4 ? T(1.0e28) : T(1.0e250);
+    constexpr T kShrink = sizeof(T) == 4 ? T(1.0e-28) : T(1.0e-250);
     const GroupDev g = groups[blockIdx.y];
     const int n = g.n;
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -125,57 +179,57 @@ __global__ void k_sph_radial(const PairDev *pairs, const GroupDev *groups, const
     const int b = (int)(idx / n), a = (int)(idx % n);
     const PairDev &P = pairs[g.pair];
     const int L = P.L;
-    const double s = P.sigma;
-    const double r1 = ra[g.slot0 + a], r2 = rb[g.slot0 + b];
+    const double r1d = ra[g.slot0 + a], r2d = rb[g.slot0 + b];
     T *out = W + g.w0 + (long long)b * n + a;
     const long long lstride = (long long)n * n;
-    if (cutoff && !(fabs(r1 - r2) < 4.0 * s)) {
+    if (cutoff && !(fabs(r1d - r2d) < 4.0 * P.sigma)) {
         for (int l = 0; l <= L; ++l) out[l * lstride] = T(0);
         return;
     }
-    const double pre = 4.0 * 17.493418327624862 /* pi^2.5 */ * s * s * s *
-                       exp(-(r1 - r2) * (r1 - r2) / (4.0 * s * s));
-    const double x = r1 * r2 / (2.0 * s * s);
-    if (x < 1.0e-6) {
-        double t = exp(-x);
+    const T s = T(P.sigma), r1 = T(r1d), r2 = T(r2d);
+    const T pre = T(4.0 * 17.493418327624862) /* 4 pi^2.5 */ * s * s * s *
+                  exp(-(r1 - r2) * (r1 - r2) / (T(4) * s * s));
+    const T x = r1 * r2 / (T(2) * s * s);
+    if (x < T(1.0e-6)) {
+        T t = exp(-x);
         for (int l = 0; l <= L; ++l) {
-            if (l > 0) t *= x / (2.0 * l + 1.0);
-            out[l * lstride] = T(pre * t * (1.0 + x * x / (2.0 * (2.0 * l + 3.0))));
+            if (l > 0) t *= x / (T(2) * l + T(1));
+            out[l * lstride] = pre * t * (T(1) + x * x / (T(2) * (T(2) * l + T(3))));
         }
         return;
     }
-    if (x >= 1000.0 && x >= (double)L * L) {
+    if (x >= T(1000) && x >= T(L) * T(L)) {
         // e^{-x} i_l(x) = (1/2x) sum_{k<=l} (l+k)!/(k!(l-k)!) (-1/2x)^k  (+ O(e^{-2x}));
         // terms shrink at least by half when x >= l^2, so the sum is stable.
         for (int l = 0; l <= L; ++l) {
-            double term = 1.0, sum = 1.0;
+            T term = 1, sum = 1;
             for (int k = 0; k < l; ++k) {
-                term *= -(double)(l + k + 1) * (double)(l - k) / ((k + 1.0) * 2.0 * x);
+                term *= -T(l + k + 1) * T(l - k) / ((T(k) + T(1)) * T(2) * x);
                 sum += term;
             }
-            out[l * lstride] = T(pre * sum / (2.0 * x));
+            out[l * lstride] = pre * sum / (T(2) * x);
         }
         return;
     }
-    double vals[64];
-    const int n0 = L + 10 + (int)(0.8 * x);
-    const double invx = 1.0 / x;
-    double fp1 = 0.0, f = 1.0;
+    T vals[64];
+    const int n0 = L + 10 + (int)(T(0.8) * x);
+    const T invx = T(1) / x;
+    T fp1 = 0, f = 1;
     for (int k = n0; k >= 1; --k) {
         if (k <= L) vals[k] = f;
-        double fm1 = (2.0 * k + 1.0) * invx * f + fp1;
-        if (fabs(fm1) > 1.0e250) {
-            fm1 *= 1.0e-250;
-            f *= 1.0e-250;
-            for (int q = k; q <= L; ++q) vals[q] *= 1.0e-250;
+        T fm1 = (T(2) * k + T(1)) * invx * f + fp1;
+        if (fabs(fm1) > kBig) {
+            fm1 *= kShrink;
+            f *= kShrink;
+            for (int q = k; q <= L; ++q) vals[q] *= kShrink;
         }
         fp1 = f;
         f = fm1;
     }
     vals[0] = f;
-    const double s0 = -expm1(-2.0 * x) / (2.0 * x);
-    const double scale = pre * s0 / f;
-    for (int l = 0; l <= L; ++l) out[l * lstride] = T(vals[l] * scale);
+    const T s0 = -expm1(T(-2) * x) / (T(2) * x);
+    const T scale = pre * s0 / f;
+    for (int l = 0; l <= L; ++l) out[l * lstride] = vals[l] * scale;
 }
 
 // ---------------------------------------------------------------------------
@@ -289,12 +343,13 @@ __global__ void k_wigner_table(int bw, double *d64, float *d32) {
     const int k = t / (W * W), i1 = (t / W) % W, i2 = t % W;
     const int m1 = (i1 < bw) ? i1 : i1 - W, m2 = (i2 < bw) ? i2 : i2 - W;
     const int l0 = max(abs(m1), abs(m2));
-    double *o64 = d64 + (long long)t * bw;
-    float *o32 = d32 ? d32 + (long long)t * bw : nullptr;
-    for (int l = 0; l < l0; ++l) {
-        o64[l] = 0.0;
-        if (o32) o32[l] = 0.f;
-    }
+    // layout [k][l][m1][m2]: element l of this (k, m1, m2) at base + l W^2
+    const long long W2 = (long long)W * W, base = (long long)k * bw * W2 + (long long)i1 * W + i2;
+    auto put = [&](int l, double v) {
+        d64[base + l * W2] = v;
+        if (d32) d32[base + l * W2] = (float)v;
+    };
+    for (int l = 0; l < l0; ++l) put(l, 0.0);
     const double beta = FO_PI * (2.0 * k + 1.0) / (4.0 * bw);
     double c = cos(beta / 2), s = sin(beta / 2), cb = cos(beta);
     int M, pc, ps;
@@ -309,8 +364,7 @@ __global__ void k_wigner_table(int bw, double *d64, float *d32) {
     for (int q = 0; q < pc; ++q) seed *= c;
     for (int q = 0; q < ps; ++q) seed *= sv;
     double prev = 0.0, cur = seed;
-    o64[l0] = cur;
-    if (o32) o32[l0] = (float)cur;
+    put(l0, cur);
     for (int l = l0; l <= bw - 2; ++l) {
         double dl = l, a = 0.0, cc = 0.0;
         double t5 = 1.0 / sqrt(((dl + 1) * (dl + 1) - (double)m1 * m1) * ((dl + 1) * (dl + 1) - (double)m2 * m2));
@@ -323,58 +377,75 @@ __global__ void k_wigner_table(int bw, double *d64, float *d32) {
         double nxt = bb * (cb - cc) * cur - a * prev;
         prev = cur;
         cur = nxt;
-        o64[l + 1] = cur;
-        if (o32) o32[l + 1] = (float)cur;
+        put(l + 1, cur);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Inverse SO(3) transform, one block per (beta index k, orientation, pair):
+// Inverse SO(3) transform, one block per (beta index k, pair) for both
+// orientations:
 //   S[m1][m2] = sum_{l >= max(|m1|,|m2|)} d^l_{m1m2}(beta_k) (+-1)^l I^l_{m1m2}
-// (the inverted copy of A has I^l -> (-1)^l I^l since Y_lm(-r) = (-1)^l Y_lm(r))
-// then unnormalised backward DFTs m2 -> gamma and m1 -> alpha in shared memory
-// and the real part written to grid[grid0 + o*G^3 + a + G*(k + G*g)].
+// (the inverted copy of A has I^l -> (-1)^l I^l since Y_lm(-r) = (-1)^l Y_lm(r),
+// so the even-l and odd-l partial sums give both), then unnormalised backward
+// DFTs m2 -> gamma and m1 -> alpha in shared memory and the real part written
+// to grid[grid0 + o*G^3 + a + G*(k + G*g)].  The Wigner table and the
+// coefficients are both [l][m1][m2], so a warp reads them contiguously.
 template <typename T, typename T2>
 __global__ void __launch_bounds__(256) k_isoft(const PairDev *pairs, const T2 *coef,
                                                const T *const *dtab, T *grid) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int k = blockIdx.x, o = blockIdx.y, p = blockIdx.z;
+    const int k = blockIdx.x, p = blockIdx.y;
     const PairDev P = pairs[p];
-    const int G = P.G, L = P.L, bw = L + 1, Wc = 2 * L + 1;
-    if (k >= G || o >= P.norient) return;
-    T2 *bufA = (T2 *)smem_raw, *bufB = bufA + G * G, *tw = bufB + G * G;
+    const int G = P.G, L = P.L, bw = L + 1, Wc = 2 * L + 1, W2 = Wc * Wc;
+    if (k >= G) return;
+    const bool inv = P.norient == 2;
+    T2 *bufA = (T2 *)smem_raw, *bufB = bufA + G * G, *bufC = bufB + G * G, *tw = bufC + G * G;
     for (int t = threadIdx.x; t < G; t += blockDim.x) {
-        double sn, cs;
-        sincospi(2.0 * t / G, &sn, &cs);
-        tw[t] = mk2<T2>(cs, sn);
+        T sn, cs;
+        if constexpr (sizeof(T) == 4) sincospif(2.0f * t / G, &sn, &cs);
+        else sincospi(2.0 * t / G, &sn, &cs);
+        tw[t] = pack2<T2, T>(cs, sn);
     }
-    for (int t = threadIdx.x; t < G * G; t += blockDim.x) bufA[t] = mk2<T2>(0, 0);
+    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+        bufA[t] = pack2<T2, T>(0, 0);
+        bufC[t] = pack2<T2, T>(0, 0);
+    }
     __syncthreads();
-    const T *d = dtab[bw];
+    const T *d = dtab[bw] + (long long)k * bw * W2;
     const T2 *I = coef + P.coef0;
-    for (int t = threadIdx.x; t < Wc * Wc; t += blockDim.x) {
+    for (int t = threadIdx.x; t < W2; t += blockDim.x) {
         const int i1 = t / Wc, i2 = t % Wc;
         const int m1 = (i1 <= L) ? i1 : i1 - Wc, m2 = (i2 <= L) ? i2 : i2 - Wc;
         const int l0 = max(abs(m1), abs(m2));
-        const T *dr = d + ((long long)(k * Wc + i1) * Wc + i2) * bw;
-        T sr = 0, si = 0;
-        for (int l = l0; l <= L; ++l) {
-            T2 c = I[((long long)l * Wc + i1) * Wc + i2];
-            T dv = dr[l];
-            if (o == 1 && (l & 1)) dv = -dv;
-            sr += dv * c.x;
-            si += dv * c.y;
+        T er = 0, ei = 0, orr = 0, oi = 0;   // even-l and odd-l partial sums
+        for (int l = l0 + (l0 & 1); l <= L; l += 2) {
+            const T2 c = I[(long long)l * W2 + t];
+            const T dv = d[(long long)l * W2 + t];
+            er += dv * c.x;
+            ei += dv * c.y;
         }
-        bufA[((m1 + G) % G) * G + (m2 + G) % G] = mk2<T2>(sr, si);
+        for (int l = l0 + 1 - (l0 & 1); l <= L; l += 2) {
+            const T2 c = I[(long long)l * W2 + t];
+            const T dv = d[(long long)l * W2 + t];
+            orr += dv * c.x;
+            oi += dv * c.y;
+        }
+        const int dst = ((m1 + G) % G) * G + (m2 + G) % G;
+        bufA[dst] = pack2<T2, T>(er + orr, ei + oi);
+        bufC[dst] = pack2<T2, T>(er - orr, ei - oi);
     }
     __syncthreads();
-    T2 *r1 = fft_lines(bufA, bufB, G, G, G, 1, +1, tw);       // m2 -> gamma
-    T2 *o1 = (r1 == bufA) ? bufB : bufA;
-    T2 *r2 = fft_lines(r1, o1, G, G, 1, G, +1, tw);           // m1 -> alpha
-    T *out = grid + P.grid0 + (long long)o * G * G * G + (long long)G * k;
-    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
-        const int a = t % G, g = t / G;
-        out[a + (long long)G * G * g] = r2[a * G + g].x;
+    for (int o = 0; o < (inv ? 2 : 1); ++o) {
+        T2 *src = o ? bufC : bufA, *scr = bufB;
+        T2 *r1 = fft_lines(src, scr, G, G, G, 1, +1, tw);       // m2 -> gamma
+        T2 *o1 = (r1 == src) ? scr : src;
+        T2 *r2 = fft_lines(r1, o1, G, G, 1, G, +1, tw);         // m1 -> alpha
+        T *out = grid + P.grid0 + (long long)o * G * G * G + (long long)G * k;
+        for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+            const int a = t % G, g = t / G;
+            out[a + (long long)G * G * g] = r2[a * G + g].x;
+        }
+        __syncthreads();
     }
 }
 
@@ -388,13 +459,13 @@ void launch_sph_center(const SphBuffers &b, cudaStream_t s) {
 void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s) {
     int nth = 2 * b.nslots, bs = 128;
     if (fp32)
-        k_sph_ylm<float2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra,
-                                                            b.rb, (float2 *)b.ylmA, (float2 *)b.ylmB,
-                                                            b.nslots);
+        k_sph_ylm<float, float2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra,
+                                                                   b.rb, (float2 *)b.ylmA,
+                                                                   (float2 *)b.ylmB, b.nslots);
     else
-        k_sph_ylm<double2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra,
-                                                             b.rb, (double2 *)b.ylmA,
-                                                             (double2 *)b.ylmB, b.nslots);
+        k_sph_ylm<double, double2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb,
+                                                                     b.ra, b.rb, (double2 *)b.ylmA,
+                                                                     (double2 *)b.ylmB, b.nslots);
 }
 
 void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s) {
@@ -424,14 +495,14 @@ void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s) {
 }
 
 void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s) {
-    dim3 grid(b.maxG, 2, b.npairs);
+    dim3 grid(b.maxG, b.npairs);
     if (fp32) {
-        size_t sm = sizeof(float2) * (2 * b.maxG * b.maxG + b.maxG);
+        size_t sm = sizeof(float2) * (3 * b.maxG * b.maxG + b.maxG);
         cudaFuncSetAttribute(k_isoft<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_isoft<float, float2><<<grid, 256, sm, s>>>(b.pairs, (const float2 *)b.coef,
                                                     (const float *const *)b.dtab, (float *)b.grid);
     } else {
-        size_t sm = sizeof(double2) * (2 * b.maxG * b.maxG + b.maxG);
+        size_t sm = sizeof(double2) * (3 * b.maxG * b.maxG + b.maxG);
         cudaFuncSetAttribute(k_isoft<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_isoft<double, double2><<<grid, 256, sm, s>>>(b.pairs, (const double2 *)b.coef,
                                                       (const double *const *)b.dtab, (double *)b.grid);
