@@ -504,7 +504,8 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     r.buckets = pl->buckets.data();
     r.nbuckets = (int)pl->buckets.size();
     r.fp32 = pl->fp32;
-    r.recomp = pl->fp32 && !pl->bulk;
+    r.recomp = pl->fp32;
+    r.bulk = pl->bulk;
     pl->d_pstatus = r.pstatus;
     pl->d_npeaks = r.npeaks;
     return FO_OK;
@@ -689,7 +690,7 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
         }
         {
             double dmax = 0.5 * std::sqrt(q.box[0] * q.box[0] + q.box[1] * q.box[1] + q.box[2] * q.box[2]);
-            RefAssign ra = ref_assign(n, maxg, pl->fp32, false, dmax);
+            RefAssign ra = ref_assign(n, maxg, pl->fp32, pl->fp32, dmax);
             P.lapstride = ra.lapstride;
             P.lap0 = lap_total;
             lap_total += (long long)P.nrot * P.lapstride;

@@ -27,35 +27,90 @@ __global__ void k_bulk_prep(const PairDev *pairs, const int *slot2orig, const do
 }
 
 // F(k) = sum_groups C^B(k) conj(C^A(k)) exp(-|k|^2 s^2), C(k) = sum_j exp(-i k.r_j),
-// one thread per wave vector; written at [ix + M(iy + M iz)] of the M^3 grid.
+// written at [ix + M(iy + M iz)] of the M^3 grid.  The phase factor separates,
+// exp(-i k.r) = e_x(ix) e_y(iy) e_z(iz) with e_a(i) = exp(-i 2 pi (i-K) r_a / L_a),
+// so a block -- one z wave number iz and a slab of up to kSfPer*256 (ix, iy)
+// wave vectors -- computes each atom's 2(2K+1)+1 axis factors once into
+// shared memory (chunks of atoms) and every wave vector then costs two complex
+// products per atom.  Factors come from sincos in the grid precision T.
+constexpr int kSfThreads = 256, kSfPer = 4, kSfSlab = kSfThreads * kSfPer;
+
+__host__ __device__ inline int sf_chunk(int nk, int tsize) {
+    // atoms per shared-memory chunk: both structures, 2nk+1 factors each, <= 48 KB
+    int c = (48 * 1024) / (2 * (2 * nk + 1) * 2 * tsize);
+    return c < 1 ? 1 : (c > 64 ? 64 : c);
+}
+
 template <typename T, typename T2>
-__global__ void k_bulk_sf(const PairDev *pairs, const GroupDev *groups, const double *xa,
-                          const double *xb, T2 *fgrid) {
+__global__ void __launch_bounds__(kSfThreads) k_bulk_sf(const PairDev *pairs, const GroupDev *groups,
+                                                        const double *xa, const double *xb, T2 *fgrid,
+                                                        int nslab) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const PairDev &P = pairs[blockIdx.y];
-    const int K = P.L, nk = 2 * K + 1, M = P.G;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nk * nk * nk) return;
-    const int ix = t % nk, iy = (t / nk) % nk, iz = t / (nk * nk);
-    const double kx = 2.0 * FO_PI / P.box[0] * (ix - K), ky = 2.0 * FO_PI / P.box[1] * (iy - K),
-                 kz = 2.0 * FO_PI / P.box[2] * (iz - K);
-    const double damp = exp(-(kx * kx + ky * ky + kz * kz) * P.sigma * P.sigma);
-    T fr = 0, fi = 0;
+    const int K = P.L, nk = 2 * K + 1, M = P.G, nf = 2 * nk + 1;
+    const int iz = blockIdx.x / nslab, slab = blockIdx.x % nslab;
+    if (iz >= nk || slab * kSfSlab >= nk * nk) return;
+    const int chunk = sf_chunk(nk, (int)sizeof(T));
+    T2 *fac = (T2 *)smem_raw;   // [side][atom][factor]: x factors 0..nk-1, y nk..2nk-1, z 2nk
+    const double twopi_l[3] = {2.0 * FO_PI / P.box[0], 2.0 * FO_PI / P.box[1], 2.0 * FO_PI / P.box[2]};
+    int ixy[kSfPer];
+#pragma unroll
+    for (int q = 0; q < kSfPer; ++q) {
+        const int w = slab * kSfSlab + q * kSfThreads + threadIdx.x;
+        ixy[q] = w < nk * nk ? w : -1;
+    }
+    T fr[kSfPer], fi[kSfPer];
+#pragma unroll
+    for (int q = 0; q < kSfPer; ++q) fr[q] = fi[q] = 0;
     for (int gi = 0; gi < P.ngroups; ++gi) {
         const GroupDev g = groups[P.group0 + gi];
-        T ar = 0, ai = 0, br = 0, bi = 0;
-        for (int j = 0; j < g.n; ++j) {
-            const double *a = xa + 3LL * (g.slot0 + j), *b = xb + 3LL * (g.slot0 + j);
-            double sa, ca, sb, cb;
-            sincos(kx * a[0] + ky * a[1] + kz * a[2], &sa, &ca);
-            sincos(kx * b[0] + ky * b[1] + kz * b[2], &sb, &cb);
-            ar += T(ca); ai -= T(sa);
-            br += T(cb); bi -= T(sb);
+        T ar[kSfPer], ai[kSfPer], br[kSfPer], bi[kSfPer];
+#pragma unroll
+        for (int q = 0; q < kSfPer; ++q) ar[q] = ai[q] = br[q] = bi[q] = 0;
+        for (int j0 = 0; j0 < g.n; j0 += chunk) {
+            const int nj = min(chunk, g.n - j0);
+            __syncthreads();   // the previous chunk's factors are no longer read
+            for (int t = threadIdx.x; t < 2 * nj * nf; t += blockDim.x) {
+                const int side = t / (nj * nf), r = t % (nj * nf), jj = r / nf, w = r % nf;
+                const double *X = (side ? xb : xa) + 3LL * (g.slot0 + j0 + jj);
+                const int axis = w < nk ? 0 : (w < 2 * nk ? 1 : 2);
+                const int m = (axis == 0 ? w : (axis == 1 ? w - nk : iz)) - K;
+                const double ph = twopi_l[axis] * m * X[axis];
+                T sn, cs;
+                if constexpr (sizeof(T) == 4) sincosf((float)ph, &sn, &cs);
+                else sincos(ph, &sn, &cs);
+                fac[(side * chunk + jj) * nf + w] = pack2<T2, T>(cs, -sn);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < kSfPer; ++q) {
+                if (ixy[q] < 0) continue;
+                const int ix = ixy[q] % nk, iy = ixy[q] / nk;
+                for (int jj = 0; jj < nj; ++jj) {
+                    const T2 *fa = fac + jj * nf, *fb = fac + (chunk + jj) * nf;
+                    const T2 ea = cmul(cmul(fa[ix], fa[nk + iy]), fa[2 * nk]);
+                    const T2 eb = cmul(cmul(fb[ix], fb[nk + iy]), fb[2 * nk]);
+                    ar[q] += ea.x; ai[q] += ea.y;
+                    br[q] += eb.x; bi[q] += eb.y;
+                }
+            }
         }
         // C^B * conj(C^A)
-        fr += br * ar + bi * ai;
-        fi += bi * ar - br * ai;
+#pragma unroll
+        for (int q = 0; q < kSfPer; ++q) {
+            fr[q] += br[q] * ar[q] + bi[q] * ai[q];
+            fi[q] += bi[q] * ar[q] - br[q] * ai[q];
+        }
     }
-    fgrid[P.coef0 + ix + (long long)M * (iy + (long long)M * iz)] = mk2<T2>(fr * damp, fi * damp);
+#pragma unroll
+    for (int q = 0; q < kSfPer; ++q) {
+        if (ixy[q] < 0) continue;
+        const int ix = ixy[q] % nk, iy = ixy[q] / nk;
+        const double kx = twopi_l[0] * (ix - K), ky = twopi_l[1] * (iy - K), kz = twopi_l[2] * (iz - K);
+        const double damp = exp(-(kx * kx + ky * ky + kz * kz) * P.sigma * P.sigma);
+        fgrid[P.coef0 + ix + (long long)M * (iy + (long long)M * iz)] =
+            pack2<T2, T>(T(fr[q] * damp), T(fi[q] * damp));
+    }
 }
 
 // One pass of the 3-D FFT: forward 1-D transforms along `axis` for a batch
@@ -105,12 +160,17 @@ void launch_bulk_prep(const BulkBuffers &b, cudaStream_t s) {
 }
 
 void launch_bulk_sf(const BulkBuffers &b, bool fp32, cudaStream_t s) {
-    int nk = 2 * b.maxK + 1, nk3 = nk * nk * nk;
-    dim3 grid((nk3 + 127) / 128, b.npairs);
-    if (fp32)
-        k_bulk_sf<float, float2><<<grid, 128, 0, s>>>(b.pairs, b.groups, b.xa, b.xb, (float2 *)b.fgrid);
-    else
-        k_bulk_sf<double, double2><<<grid, 128, 0, s>>>(b.pairs, b.groups, b.xa, b.xb, (double2 *)b.fgrid);
+    const int nk = 2 * b.maxK + 1, nslab = (nk * nk + kSfSlab - 1) / kSfSlab;
+    dim3 grid(nk * nslab, b.npairs);
+    if (fp32) {
+        const size_t sm = sizeof(float2) * 2 * sf_chunk(nk, 4) * (2 * nk + 1);
+        k_bulk_sf<float, float2><<<grid, kSfThreads, sm, s>>>(b.pairs, b.groups, b.xa, b.xb,
+                                                             (float2 *)b.fgrid, nslab);
+    } else {
+        const size_t sm = sizeof(double2) * 2 * sf_chunk(nk, 8) * (2 * nk + 1);
+        k_bulk_sf<double, double2><<<grid, kSfThreads, sm, s>>>(b.pairs, b.groups, b.xa, b.xb,
+                                                               (double2 *)b.fgrid, nslab);
+    }
 }
 
 void launch_bulk_fft(const BulkBuffers &b, bool fp32, cudaStream_t s) {

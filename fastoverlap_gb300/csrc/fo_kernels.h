@@ -77,7 +77,8 @@ struct RefineBuffers {
     const RefineBucket *buckets;   // host
     int nbuckets;
     bool fp32;
-    bool recomp;   // costs recomputed from FP32 coordinates (mixed cluster form)
+    bool recomp;   // costs recomputed from FP32 coordinates (mixed form)
+    bool bulk;     // periodic pairs (minimum-image distances)
 };
 void launch_findpeaks(const RefineBuffers &b, bool fp32, cudaStream_t s);
 void launch_findpeaks_from(const PairDev *pairs, int npairs, void *grid, double *omax, double *peaks,

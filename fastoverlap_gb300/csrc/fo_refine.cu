@@ -10,10 +10,10 @@
 // Candidates are launched in buckets of equal shared-memory footprint so
 // small problems pack many warps per SM; the assignment arrays live in
 // shared memory when they fit and in per-candidate global scratch otherwise.
-// In the mixed-precision cluster form the costs are not stored: the
-// assignment recomputes each one from the FP32 coordinates (float4 per atom)
-// where it reads it, which keeps the per-warp footprint small enough for
-// many warps per SM.
+// In the mixed-precision form the costs are not stored: the assignment
+// recomputes each one from the FP32 coordinates (float4 per atom) where it
+// reads it, which keeps the per-warp footprint small enough for many warps
+// per SM.
 //
 // Reference behaviour (matthewghgriffiths/fastoverlap):
 //   ITERATIVEALIGN   fastoverlap/f90/alignutils.f90:111-286
@@ -103,11 +103,16 @@ struct CostStored {      // costs kept in a row-major table of width m
     __device__ __forceinline__ long long operator()(int i, int t, int) const { return (long long)cc[i * m + t]; }
 };
 
-template <typename CT>
-struct CostF32 {         // cluster costs recomputed from FP32 coordinates
+template <typename CT, bool BOX>
+struct CostF32 {         // costs recomputed from FP32 coordinates (minimum image when BOX)
     const float4 *b, *a;
+    float bx[3];
+    __device__ __forceinline__ float d2(int i, int j) const {
+        if constexpr (BOX) return d2_f4_box(b[i], a[j], bx);
+        else return d2_f4(b[i], a[j]);
+    }
     __device__ __forceinline__ long long operator()(int i, int, int j) const {
-        return (long long)cost_of_f32<CT>(d2_f4(b[i], a[j]));
+        return (long long)cost_of_f32<CT>(d2(i, j));
     }
 };
 
@@ -512,7 +517,7 @@ struct GroupCoords {
 
 // Neighbour lists / costs of one group, then its assignment (PAIRDISTS +
 // JOVOSAP for one group).  Returns the assignment's status.
-template <typename KT, typename DT, typename CT, bool RECOMP>
+template <typename KT, typename DT, typename CT, bool RECOMP, bool BOX>
 __device__ int assign_group(const int ns, const int m, const GroupCoords &G, unsigned char *lb,
                             const RefLayout &L) {
     const int lane = threadIdx.x & 31;
@@ -524,15 +529,16 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
     int *fr = (int *)(lb + L.lap_fr), *todo = (int *)(lb + L.lap_todo);
     unsigned char *ok = lb + L.lap_ok;
     if constexpr (RECOMP) {
-        if (!dense) {
-            float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
-            for (int i = lane; i < ns; i += 32) {
-                const float4 bi = G.B4[i];
-                nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return d2_f4(bi, G.A4[j]); });
+        auto run = [&](const auto &cf) {
+            if (!dense) {
+                float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
+                for (int i = lane; i < ns; i += 32)
+                    nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
             }
-        }
-        __syncwarp();
-        return jv_warp<!kF32, KT>(ns, m, dense, CostF32<CT>{G.B4, G.A4}, kk, v, dd, x, y, lab, fr, todo, ok);
+            __syncwarp();
+            return jv_warp<!kF32, KT>(ns, m, dense, cf, kk, v, dd, x, y, lab, fr, todo, ok);
+        };
+        return run(CostF32<CT, BOX>{G.B4, G.A4, {G.bxf[0], G.bxf[1], G.bxf[2]}});
     } else {
         CT *cc = (CT *)(lb + L.lap_cc);
         // squared distance of row i (bi: its FP64 coordinates) and column j
@@ -593,7 +599,7 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
 // the candidate's output slot (cxyz); the fixed structure and the rotated
 // starting structure are recomputed from the inputs where they are read, with
 // the same expressions as when they are first formed.
-template <typename DT, typename CT, bool RECOMP>
+template <typename DT, typename CT, bool RECOMP, bool BOX>
 __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
     const double *xa, const double *xb, const double *peaks, const int *npeaks, unsigned char *lapg,
@@ -698,8 +704,8 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
             GC.A = DA + 3 * s0;
             GC.B4 = B4 + s0;
             GC.A4 = A4 + s0;
-            const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP>(ns, m, GC, lb, L)
-                                            : assign_group<uint16_t, DT, CT, RECOMP>(ns, m, GC, lb, L);
+            const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L)
+                                            : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L);
             if (rc) fail += 1;
             __syncwarp();
             for (int i = lane; i < ns; i += 32) {
@@ -939,20 +945,28 @@ void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux,
         if (bk.count == 0) continue;
         const int *list = b.cand_list + bk.offset;
         cudaStream_t s = naux ? aux[k % naux] : main;
-#define FO_LAUNCH_REFINE(DT, CT, RC)                                                                 \
-    do {                                                                                            \
-        cudaFuncSetAttribute(k_refine_warp<DT, CT, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             (int)bk.smem);                                                         \
-        k_refine_warp<DT, CT, RC><<<bk.count, 32, bk.smem, s>>>(                                    \
-            b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,    \
-            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);                                     \
+#define FO_LAUNCH_REFINE(DT, CT, RC, BX)                                                              \
+    do {                                                                                              \
+        cudaFuncSetAttribute(k_refine_warp<DT, CT, RC, BX>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)bk.smem);                                                           \
+        k_refine_warp<DT, CT, RC, BX><<<bk.count, 32, bk.smem, s>>>(                                  \
+            b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,      \
+            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);                                       \
     } while (0)
         if (b.fp32 && b.recomp) {
-            if (bk.ct64) FO_LAUNCH_REFINE(float, long long, true); else FO_LAUNCH_REFINE(float, int, true);
+            if (b.bulk) {
+                if (bk.ct64) FO_LAUNCH_REFINE(float, long long, true, true);
+                else FO_LAUNCH_REFINE(float, int, true, true);
+            } else {
+                if (bk.ct64) FO_LAUNCH_REFINE(float, long long, true, false);
+                else FO_LAUNCH_REFINE(float, int, true, false);
+            }
         } else if (b.fp32) {
-            if (bk.ct64) FO_LAUNCH_REFINE(float, long long, false); else FO_LAUNCH_REFINE(float, int, false);
+            if (bk.ct64) FO_LAUNCH_REFINE(float, long long, false, false);
+            else FO_LAUNCH_REFINE(float, int, false, false);
         } else {
-            if (bk.ct64) FO_LAUNCH_REFINE(double, long long, false); else FO_LAUNCH_REFINE(double, int, false);
+            if (bk.ct64) FO_LAUNCH_REFINE(double, long long, false, false);
+            else FO_LAUNCH_REFINE(double, int, false, false);
         }
 #undef FO_LAUNCH_REFINE
     }
