@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -62,6 +63,11 @@ struct fo_ctx {
     cudaEvent_t fork = nullptr, join[kAux] = {};
     void *flush_buf = nullptr;
     size_t flush_bytes = 0;
+    // device memory of the largest destroyed plan, handed to the next plan
+    // that fits (a batch call then allocates nothing after the first)
+    unsigned char *arena = nullptr;
+    size_t arena_bytes = 0;
+    bool arena_busy = false;
 };
 
 struct fo_plan {
@@ -75,6 +81,7 @@ struct fo_plan {
     std::vector<long long> caller_off;  // caller's atom offset per pair
     unsigned char *dmem = nullptr;
     size_t dbytes = 0;
+    bool from_arena = false;
     fo::SphBuffers sb{};
     fo::BulkBuffers bb{};
     fo::RefineBuffers rb{};
@@ -186,14 +193,25 @@ void rec_event(fo_plan *pl, int kid) {
 }
 
 fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
-    size_t budget = ctx->opts.hbm_budget_bytes;
-    if (budget == 0) {
+    // the caller's budget bounds every plan; the automatic one (80% of the
+    // free memory) only what still has to be allocated
+    const size_t user = ctx->opts.hbm_budget_bytes;
+    if (user && bytes > user)
+        return set_err(ctx, FO_ERR_OOM_BUDGET, "plan needs %zu bytes, budget %zu", bytes, user);
+    if (ctx->arena && !ctx->arena_busy && ctx->arena_bytes >= bytes) {
+        pl->dmem = ctx->arena;
+        pl->dbytes = bytes;
+        pl->from_arena = true;
+        ctx->arena_busy = true;
+        return FO_OK;
+    }
+    if (!user) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        budget = (size_t)(0.8 * fr);
+        if (bytes > (size_t)(0.8 * fr))
+            return set_err(ctx, FO_ERR_OOM_BUDGET, "plan needs %zu bytes, 80%% of free memory is %zu", bytes,
+                           (size_t)(0.8 * fr));
     }
-    if (bytes > budget)
-        return set_err(ctx, FO_ERR_OOM_BUDGET, "plan needs %zu bytes, budget %zu", bytes, budget);
     fo_status s = cuda_check(ctx, cudaMalloc(&pl->dmem, bytes), "cudaMalloc(plan)");
     if (s) return s;
     pl->dbytes = bytes;
@@ -239,20 +257,14 @@ RefAssign ref_assign(int n, int maxg, bool fp32, bool recomp, double dmax) {
     return r;
 }
 
-int cand2pair_of(const fo_plan *pl, int c) {
-    // candidates of pair i are [cand0, cand0 + norient*nrot)
-    int lo = 0, hi = (int)pl->hp.size() - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) / 2;
-        if (pl->hp[mid].cand0 <= c) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 void build_buckets(fo_plan *pl, const std::vector<RefAssign> &ra, std::vector<int> &cand_list) {
+    // within a class, heavier (more atoms) candidates first so the tail of
+    // each launch is short; pairs of equal size keep their order
+    std::vector<int> order(pl->hp.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pl->hp[a].n > pl->hp[b].n; });
     std::map<std::pair<int, size_t>, std::vector<int>> by;
-    for (size_t i = 0; i < pl->hp.size(); ++i) {
+    for (int i : order) {
         const fo::PairDev &P = pl->hp[i];
         auto &v = by[{ra[i].ct64, ra[i].smem}];
         for (int c = 0; c < P.norient * P.nrot; ++c) v.push_back(P.cand0 + c);
@@ -263,10 +275,6 @@ void build_buckets(fo_plan *pl, const std::vector<RefAssign> &ra, std::vector<in
     // own stream, and the longest launches start at once
     for (auto it = by.rbegin(); it != by.rend(); ++it) {
         auto &kv = *it;
-        // heavier candidates first so the tail of each launch is short
-        std::stable_sort(kv.second.begin(), kv.second.end(), [&](int x, int y) {
-            return pl->hp[cand2pair_of(pl, x)].n > pl->hp[cand2pair_of(pl, y)].n;
-        });
         fo::RefineBucket b;
         b.offset = (int)cand_list.size();
         b.count = (int)kv.second.size();
@@ -369,6 +377,7 @@ void fo_ctx_destroy(fo_ctx *ctx) {
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     cudaFree(ctx->flush_buf);
+    cudaFree(ctx->arena);
     for (int a = 0; a < fo_ctx::kAux; ++a) {
         if (ctx->aux[a]) cudaStreamDestroy(ctx->aux[a]);
         if (ctx->join[a]) cudaEventDestroy(ctx->join[a]);
@@ -821,7 +830,16 @@ void fo_plan_destroy(fo_plan *pl) {
     cudaSetDevice(pl->ctx->opts.device);
     cudaStreamSynchronize(pl->ctx->stream);
     for (auto e : pl->evs) cudaEventDestroy(e);
-    cudaFree(pl->dmem);
+    fo_ctx *ctx = pl->ctx;
+    if (pl->from_arena) {
+        ctx->arena_busy = false;
+    } else if (!ctx->arena_busy && pl->dbytes > ctx->arena_bytes) {
+        cudaFree(ctx->arena);   // keep the larger block
+        ctx->arena = pl->dmem;
+        ctx->arena_bytes = pl->dbytes;
+    } else {
+        cudaFree(pl->dmem);
+    }
     delete pl;
 }
 

@@ -136,7 +136,12 @@ fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
 
 /* ---- resident plans: upload once, run many times (inputs stay in HBM) ----
  * fo_plan_run launches the whole pipeline on the context's stream and
- * returns without synchronising; fo_plan_wait blocks until it is done.      */
+ * returns without synchronising; fo_plan_wait blocks until it is done.
+ * A plan's device memory is one block.  When a plan is destroyed the context
+ * keeps its block if it is the largest so far (freed by fo_ctx_destroy) and
+ * hands it to the next plan that fits, so repeated batch calls allocate no
+ * device memory.  A caller's hbm_budget_bytes bounds every plan; the
+ * automatic budget (80% of free memory) applies to new allocations only.   */
 typedef struct fo_plan fo_plan;
 fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
                                  const double *pos1, const double *pos2,
