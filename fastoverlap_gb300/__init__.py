@@ -8,13 +8,16 @@ Batched and resident forms:
     align_clusters, align_periodic, ClusterBatch, BulkBatch
 Peak search on an overlap grid (the Fortran FINDPEAKS):
     findpeaks
+Serving (requests admitted as they arrive, continuous batching):
+    Server
 All compute runs in libfastoverlap_gb300.so (CUDA); there is no CPU path.
 """
 from ._lib import Context, FoError, default_context, load  # noqa: F401
 from .batch import BulkBatch, ClusterBatch, align_clusters, align_periodic, findpeaks  # noqa: F401
+from .serve import Server  # noqa: F401
 from .periodicAlignment import PeriodicAlign, PeriodicAlignFortran  # noqa: F401
 from .sphericalAlignment import SphericalAlign, SphericalAlignFortran  # noqa: F401
 
 __all__ = ["SphericalAlign", "SphericalAlignFortran", "PeriodicAlign", "PeriodicAlignFortran",
-           "align_clusters", "align_periodic", "ClusterBatch", "BulkBatch", "findpeaks", "Context",
+           "align_clusters", "align_periodic", "ClusterBatch", "BulkBatch", "findpeaks", "Server", "Context",
            "FoError", "default_context", "load"]

@@ -55,6 +55,28 @@ class FoPairResult(ctypes.Structure):
                 ("status", ctypes.c_int), ("niter", ctypes.c_int)]
 
 
+class FoRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("natoms", ctypes.c_int), ("ngroups", ctypes.c_int),
+                ("jmax", ctypes.c_int), ("nrot", ctypes.c_int), ("invert", ctypes.c_int),
+                ("nwave", ctypes.c_int), ("nfspace", ctypes.c_int), ("sigma", ctypes.c_double),
+                ("box", ctypes.c_double * 3), ("pos1", ctypes.POINTER(ctypes.c_double)),
+                ("pos2", ctypes.POINTER(ctypes.c_double)), ("perm", ctypes.POINTER(ctypes.c_int)),
+                ("group_sizes", ctypes.POINTER(ctypes.c_int))]
+
+
+class FoServerOpts(ctypes.Structure):
+    _fields_ = [("max_batch", ctypes.c_int), ("max_queue", ctypes.c_int),
+                ("max_wait_ms", ctypes.c_double)]
+
+
+class FoServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("failed", ctypes.c_int64), ("batches", ctypes.c_int64),
+                ("latency_p50_ms", ctypes.c_double), ("latency_p99_ms", ctypes.c_double),
+                ("latency_max_ms", ctypes.c_double), ("mean_batch", ctypes.c_double),
+                ("busy_ms", ctypes.c_double)]
+
+
 RESULT_DTYPE = np.dtype([("dist", "f8"), ("rmat", "f8", (9,)), ("disp", "f8", (3,)),
                          ("overlap_max", "f8"), ("sigma", "f8"), ("inverted", "i4"),
                          ("ncand", "i4"), ("status", "i4"), ("niter", "i4")])
@@ -110,6 +132,14 @@ EXPORTS = {
                                          ctypes.POINTER(ctypes.c_float)]),
     "fo_ctx_flush_l2": (ctypes.c_int, [_vp, ctypes.c_size_t]),
     "fo_ctx_synchronize": (ctypes.c_int, [_vp]),
+    "fo_server_create": (ctypes.c_int, [_vp, ctypes.POINTER(FoServerOpts), ctypes.POINTER(_vp)]),
+    "fo_server_submit": (ctypes.c_int, [_vp, ctypes.POINTER(FoRequest),
+                                        ctypes.POINTER(ctypes.c_int64)]),
+    "fo_server_poll": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.POINTER(FoPairResult), _dp, _ip]),
+    "fo_server_wait": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_double,
+                                      ctypes.POINTER(FoPairResult), _dp, _ip]),
+    "fo_server_stats_get": (ctypes.c_int, [_vp, ctypes.POINTER(FoServerStats)]),
+    "fo_server_destroy": (None, [_vp]),
 }
 
 _LIB = None

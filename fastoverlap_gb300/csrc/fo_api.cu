@@ -63,11 +63,10 @@ struct fo_ctx {
     cudaEvent_t fork = nullptr, join[kAux] = {};
     void *flush_buf = nullptr;
     size_t flush_bytes = 0;
-    // device memory of the largest destroyed plan, handed to the next plan
-    // that fits (a batch call then allocates nothing after the first)
-    unsigned char *arena = nullptr;
-    size_t arena_bytes = 0;
-    bool arena_busy = false;
+    // device blocks of destroyed plans (at most kPoolMax, the largest kept),
+    // handed to later plans that fit: repeated batches allocate nothing
+    static constexpr int kPoolMax = 4;
+    std::vector<std::pair<unsigned char *, size_t>> pool;
 };
 
 struct fo_plan {
@@ -80,8 +79,7 @@ struct fo_plan {
     std::vector<fo::GroupDev> hg;
     std::vector<long long> caller_off;  // caller's atom offset per pair
     unsigned char *dmem = nullptr;
-    size_t dbytes = 0;
-    bool from_arena = false;
+    size_t dbytes = 0, block_bytes = 0;
     fo::SphBuffers sb{};
     fo::BulkBuffers bb{};
     fo::RefineBuffers rb{};
@@ -198,11 +196,14 @@ fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
     const size_t user = ctx->opts.hbm_budget_bytes;
     if (user && bytes > user)
         return set_err(ctx, FO_ERR_OOM_BUDGET, "plan needs %zu bytes, budget %zu", bytes, user);
-    if (ctx->arena && !ctx->arena_busy && ctx->arena_bytes >= bytes) {
-        pl->dmem = ctx->arena;
+    int best = -1;   // smallest pooled block that fits
+    for (int k = 0; k < (int)ctx->pool.size(); ++k)
+        if (ctx->pool[k].second >= bytes && (best < 0 || ctx->pool[k].second < ctx->pool[best].second)) best = k;
+    if (best >= 0) {
+        pl->dmem = ctx->pool[best].first;
+        pl->block_bytes = ctx->pool[best].second;
         pl->dbytes = bytes;
-        pl->from_arena = true;
-        ctx->arena_busy = true;
+        ctx->pool.erase(ctx->pool.begin() + best);
         return FO_OK;
     }
     if (!user) {
@@ -214,7 +215,7 @@ fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
     }
     fo_status s = cuda_check(ctx, cudaMalloc(&pl->dmem, bytes), "cudaMalloc(plan)");
     if (s) return s;
-    pl->dbytes = bytes;
+    pl->dbytes = pl->block_bytes = bytes;
     return FO_OK;
 }
 
@@ -377,7 +378,7 @@ void fo_ctx_destroy(fo_ctx *ctx) {
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     cudaFree(ctx->flush_buf);
-    cudaFree(ctx->arena);
+    for (auto &b : ctx->pool) cudaFree(b.first);
     for (int a = 0; a < fo_ctx::kAux; ++a) {
         if (ctx->aux[a]) cudaStreamDestroy(ctx->aux[a]);
         if (ctx->join[a]) cudaEventDestroy(ctx->join[a]);
@@ -831,14 +832,15 @@ void fo_plan_destroy(fo_plan *pl) {
     cudaStreamSynchronize(pl->ctx->stream);
     for (auto e : pl->evs) cudaEventDestroy(e);
     fo_ctx *ctx = pl->ctx;
-    if (pl->from_arena) {
-        ctx->arena_busy = false;
-    } else if (!ctx->arena_busy && pl->dbytes > ctx->arena_bytes) {
-        cudaFree(ctx->arena);   // keep the larger block
-        ctx->arena = pl->dmem;
-        ctx->arena_bytes = pl->dbytes;
-    } else {
-        cudaFree(pl->dmem);
+    if (pl->dmem) {
+        ctx->pool.push_back({pl->dmem, pl->block_bytes});
+        if ((int)ctx->pool.size() > fo_ctx::kPoolMax) {   // drop the smallest block
+            auto it = std::min_element(ctx->pool.begin(), ctx->pool.end(),
+                                       [](const std::pair<unsigned char *, size_t> &a,
+                                          const std::pair<unsigned char *, size_t> &b) { return a.second < b.second; });
+            cudaFree(it->first);
+            ctx->pool.erase(it);
+        }
     }
     delete pl;
 }

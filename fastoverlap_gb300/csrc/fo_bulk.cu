@@ -34,10 +34,12 @@ __global__ void k_bulk_prep(const PairDev *pairs, const int *slot2orig, const do
 // shared memory (chunks of atoms) and every wave vector then costs two complex
 // products per atom.  Factors come from sincos in the grid precision T.
 constexpr int kSfThreads = 256, kSfPer = 4, kSfSlab = kSfThreads * kSfPer;
+constexpr int kSfSmem = 48 * 1024;   // dynamic shared memory of every k_bulk_sf block
 
 __host__ __device__ inline int sf_chunk(int nk, int tsize) {
-    // atoms per shared-memory chunk: both structures, 2nk+1 factors each, <= 48 KB
-    int c = (48 * 1024) / (2 * (2 * nk + 1) * 2 * tsize);
+    // atoms per shared-memory chunk: both structures, 2nk+1 complex factors
+    // each, within kSfSmem for every nk (so pairs of any K share one launch)
+    int c = kSfSmem / (2 * (2 * nk + 1) * 2 * tsize);
     return c < 1 ? 1 : (c > 64 ? 64 : c);
 }
 
@@ -162,15 +164,14 @@ void launch_bulk_prep(const BulkBuffers &b, cudaStream_t s) {
 void launch_bulk_sf(const BulkBuffers &b, bool fp32, cudaStream_t s) {
     const int nk = 2 * b.maxK + 1, nslab = (nk * nk + kSfSlab - 1) / kSfSlab;
     dim3 grid(nk * nslab, b.npairs);
-    if (fp32) {
-        const size_t sm = sizeof(float2) * 2 * sf_chunk(nk, 4) * (2 * nk + 1);
-        k_bulk_sf<float, float2><<<grid, kSfThreads, sm, s>>>(b.pairs, b.groups, b.xa, b.xb,
-                                                             (float2 *)b.fgrid, nslab);
-    } else {
-        const size_t sm = sizeof(double2) * 2 * sf_chunk(nk, 8) * (2 * nk + 1);
-        k_bulk_sf<double, double2><<<grid, kSfThreads, sm, s>>>(b.pairs, b.groups, b.xa, b.xb,
-                                                               (double2 *)b.fgrid, nslab);
-    }
+    // one chunk of any pair's factors fits kSfSmem (nk <= 2K+1 <= M <= 256, so
+    // even a single atom's 2(2nk+1) FP64 factors take at most 16 KB)
+    if (fp32)
+        k_bulk_sf<float, float2><<<grid, kSfThreads, kSfSmem, s>>>(b.pairs, b.groups, b.xa, b.xb,
+                                                                  (float2 *)b.fgrid, nslab);
+    else
+        k_bulk_sf<double, double2><<<grid, kSfThreads, kSfSmem, s>>>(b.pairs, b.groups, b.xa, b.xb,
+                                                                    (double2 *)b.fgrid, nslab);
 }
 
 void launch_bulk_fft(const BulkBuffers &b, bool fp32, cudaStream_t s) {

@@ -183,26 +183,65 @@ def config3(npairs=64, seed_offset=0):
     return pairs
 
 
-def config4_stream(rate=2000.0, duration=60.0, seed_offset=0, max_requests=None):
-    """Poisson arrivals: 70% spherical (N~U{13..500}, Jmax {7,15}), 30% periodic
-    (N~U{64..1024}, density 1.2, 80:20, K {5,7}).  Yields (t_arrival, request)."""
+def _c4_base(args):
+    """One base structure of the served stream (kind, index)."""
+    kind, k, seed_offset = args
+    seed = BASE_SEED["c4"] + seed_offset + (0 if kind == "cluster" else 10 ** 5) + k
+    rng = np.random.Generator(np.random.PCG64(seed + 10 ** 7))
+    if kind == "cluster":
+        n = int(rng.integers(13, 501))
+        A = ball_points(rng, n, 1.9 * (n / 38.0) ** (1.0 / 3.0), 0.9)
+        return dict(kind=kind, pos1=A, sizes=[n], Jmax=int(rng.choice([7, 15])))
+    n = int(rng.integers(64, 1025))
+    na = int(round(0.8 * n))
+    L = (n / 1.2) ** (1.0 / 3.0)
+    A = box_points(rng, n, L, 0.8)
+    return dict(kind=kind, pos1=A, sizes=[na, n - na], box=np.array([L, L, L]),
+                nwave=int(rng.choice([5, 7])))
+
+
+def config4_pool(n_cluster=48, n_periodic=16, seed_offset=0, pool=None):
+    """Base structures of the served stream: spherical N~U{13..500} in a ball of
+    radius 1.9 (N/38)^(1/3) with minimum distance 0.9 (as config 0), periodic
+    N~U{64..1024} at density 1.2, 80:20, minimum distance 0.8 (as config 1).
+    pool: an optional multiprocessing pool (generation takes seconds per
+    large structure)."""
+    jobs = [("cluster", k, seed_offset) for k in range(n_cluster)] + \
+           [("periodic", k, seed_offset) for k in range(n_periodic)]
+    return list(pool.map(_c4_base, jobs)) if pool is not None else [_c4_base(a) for a in jobs]
+
+
+def config4_requests(bases, rate=2000.0, duration=60.0, seed_offset=0, max_requests=None):
+    """Poisson arrivals at `rate` per second: 70% spherical, 30% periodic, each
+    drawn from the base structures.  A request's B is its base A under a fresh
+    Haar rotation (spherical; inverted for half) or uniform translation mod box
+    (periodic), a random within-species permutation and N(0, 0.05^2) noise.
+    Yields (t_arrival, request dict)."""
     rng = np.random.Generator(np.random.PCG64(BASE_SEED["c4"] + seed_offset))
+    cl = [b for b in bases if b["kind"] == "cluster"]
+    pe = [b for b in bases if b["kind"] == "periodic"]
     t = 0.0
     k = 0
     while True:
         t += rng.exponential(1.0 / rate)
         if t > duration or (max_requests is not None and k >= max_requests):
             return
-        seed = BASE_SEED["c4"] + seed_offset + 1 + k
-        r2 = np.random.Generator(np.random.PCG64(seed + 10 ** 7))
-        if r2.uniform() < 0.7:
-            n = int(r2.integers(13, 501))
-            p = cluster_pair(seed, n=n, radius=1.9 * (n / 38.0) ** (1.0 / 3.0))
-            p.update(kind="cluster", Jmax=int(r2.choice([7, 15])), sigma=0.3, nrot=10)
+        b = cl[rng.integers(len(cl))] if rng.uniform() < 0.7 else pe[rng.integers(len(pe))]
+        A = b["pos1"]
+        n = len(A)
+        groups = _groups_from_sizes(b["sizes"])
+        perm = np.arange(n)
+        for g in groups:
+            perm[g] = rng.permutation(g)
+        if b["kind"] == "cluster":
+            B = (A @ haar_rotation(rng).T)[perm] + rng.normal(scale=0.05, size=A.shape)
+            if rng.uniform() < 0.5:
+                B = -B
+            req = dict(kind="cluster", pos1=A, pos2=B, perm=groups, Jmax=b["Jmax"], sigma=0.3, nrot=10)
         else:
-            n = int(r2.integers(64, 1025))
-            na = int(round(0.8 * n))
-            p = periodic_pair(seed, n=n, sizes=(na, n - na))
-            p.update(kind="periodic", sigma=0.0, nwave=int(r2.choice([5, 7])), ndisps=10)
-        yield t, p
+            L = b["box"]
+            B = np.mod(A + rng.uniform(0, L[0], size=3), L)[perm] + rng.normal(scale=0.05, size=A.shape)
+            req = dict(kind="periodic", pos1=A, pos2=B, perm=groups, box=L, sigma=0.0, nwave=b["nwave"],
+                       ndisps=10)
+        yield t, req
         k += 1

@@ -138,10 +138,10 @@ fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
  * fo_plan_run launches the whole pipeline on the context's stream and
  * returns without synchronising; fo_plan_wait blocks until it is done.
  * A plan's device memory is one block.  When a plan is destroyed the context
- * keeps its block if it is the largest so far (freed by fo_ctx_destroy) and
- * hands it to the next plan that fits, so repeated batch calls allocate no
- * device memory.  A caller's hbm_budget_bytes bounds every plan; the
- * automatic budget (80% of free memory) applies to new allocations only.   */
+ * keeps its block (up to four blocks, the largest; freed by fo_ctx_destroy)
+ * and hands the smallest one that fits to a later plan, so repeated batches
+ * allocate no device memory.  A caller's hbm_budget_bytes bounds every plan;
+ * the automatic budget (80% of free memory) applies to new allocations only. */
 typedef struct fo_plan fo_plan;
 fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
                                  const double *pos1, const double *pos2,
@@ -236,6 +236,67 @@ fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natom
 /* BULKFASTOVERLAP::CALCDEFAULTS */
 fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz,
                                double *kernelwidth, int *nwave, int *nfspace);
+
+/* ---- serving: alignment requests admitted as they arrive ----
+ * No counterpart in the reference (its classes align one pair per call).
+ * Spherical (SphericalAlign) and periodic (PeriodicAlign) requests of any
+ * size are submitted one at a time, from any host thread; inputs are copied
+ * at submission.  A worker thread gathers every request pending when the GPU
+ * is free (continuous batching, arrival order, at most max_batch), runs them
+ * as one resident plan per kind on the context's stream, and completes their
+ * tickets.  A plan larger than the context's HBM budget is split in halves;
+ * a request that does not fit alone completes with FO_ERR_OOM_BUDGET.  The
+ * server owns the context while it lives: make no other call on it.        */
+typedef struct fo_server fo_server;
+
+enum { FO_KIND_CLUSTER = 0, FO_KIND_BULK = 1 };
+
+typedef struct {
+    int           kind;        /* FO_KIND_CLUSTER or FO_KIND_BULK                  */
+    int           natoms;
+    int           ngroups;
+    int           jmax;        /* cluster: L                                       */
+    int           nrot;        /* cluster: peaks per orientation; bulk: displacements
+                                  (<= 0: 10)                                        */
+    int           invert;      /* cluster: also align the inverted copy            */
+    int           nwave;       /* bulk: K (<= 0: default)                          */
+    int           nfspace;     /* bulk: M (<= 0: default)                          */
+    double        sigma;       /* <= 0: default width                              */
+    double        box[3];      /* bulk: box lengths                                */
+    const double *pos1;        /* 3*natoms, target structure                       */
+    const double *pos2;        /* 3*natoms, structure moved onto it                */
+    const int    *perm;        /* natoms atom indices (0-based) grouped by species */
+    const int    *group_sizes; /* ngroups                                          */
+} fo_request;
+
+typedef struct {
+    int    max_batch;     /* requests per plan; <= 0: 4096                         */
+    int    max_queue;     /* pending requests before FO_ERR_QUEUE_FULL; <= 0: 1<<20 */
+    double max_wait_ms;   /* once the GPU is free, wait up to this long for more
+                             requests before launching; 0: launch at once           */
+} fo_server_opts;
+
+typedef struct {
+    int64_t submitted, completed, failed, batches;
+    double  latency_p50_ms, latency_p99_ms, latency_max_ms;  /* submit -> complete */
+    double  mean_batch;   /* requests per batch                                    */
+    double  busy_ms;      /* wall time with a batch being prepared or run           */
+} fo_server_stats;
+
+fo_status fo_server_create(fo_ctx *ctx, const fo_server_opts *opts, fo_server **out);
+/* FO_ERR_BAD_ARGS for an invalid request (nothing queued). */
+fo_status fo_server_submit(fo_server *srv, const fo_request *req, int64_t *ticket);
+/* FO_ERR_NOT_READY while the request is in flight; otherwise the request's own
+ * status, with result, aligned (3*natoms, may be NULL) and permbest (natoms,
+ * 0-based, may be NULL) filled as by the batch entry points, and the ticket
+ * released.  fo_server_wait blocks up to timeout_ms (< 0: no limit) and
+ * returns FO_ERR_TIMEOUT when the time runs out.                             */
+fo_status fo_server_poll(fo_server *srv, int64_t ticket, fo_pair_result *result, double *aligned,
+                         int *permbest);
+fo_status fo_server_wait(fo_server *srv, int64_t ticket, double timeout_ms, fo_pair_result *result,
+                         double *aligned, int *permbest);
+fo_status fo_server_stats_get(fo_server *srv, fo_server_stats *stats);
+void      fo_server_destroy(fo_server *srv);   /* completes every queued request first */
 
 /* ---- timing helpers on the context's stream (benchmarks) ----
  * fo_ctx_record records CUDA event `slot` (0..63) on the context stream;

@@ -34,16 +34,21 @@ def test_struct_layouts_match_header(tmp_path, fo):
     from fastoverlap_gb300 import _lib
     src = tmp_path / "sz.c"
     src.write_text('#include "fastoverlap_gb300.h"\n#include <stdio.h>\n#include <stddef.h>\n'
-                   'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(fo_opts),'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(fo_opts),'
                    ' sizeof(fo_cluster_pair), sizeof(fo_bulk_pair), sizeof(fo_pair_result),'
-                   ' offsetof(fo_bulk_pair, box), offsetof(fo_pair_result, inverted));return 0;}\n')
+                   ' offsetof(fo_bulk_pair, box), offsetof(fo_pair_result, inverted),'
+                   ' sizeof(fo_request), offsetof(fo_request, pos1), offsetof(fo_request, group_sizes),'
+                   ' sizeof(fo_server_opts), sizeof(fo_server_stats));return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
                                           check=True).stdout.split()]
     want = [ctypes.sizeof(_lib.FoOpts), ctypes.sizeof(_lib.FoClusterPair),
             ctypes.sizeof(_lib.FoBulkPair), ctypes.sizeof(_lib.FoPairResult),
-            _lib.FoBulkPair.box.offset, _lib.FoPairResult.inverted.offset]
+            _lib.FoBulkPair.box.offset, _lib.FoPairResult.inverted.offset,
+            ctypes.sizeof(_lib.FoRequest), _lib.FoRequest.pos1.offset,
+            _lib.FoRequest.group_sizes.offset, ctypes.sizeof(_lib.FoServerOpts),
+            ctypes.sizeof(_lib.FoServerStats)]
     assert got == want
 
 
