@@ -72,6 +72,20 @@ __device__ __forceinline__ float min_image_f(float t, float bk) {
     return bk != 0.f ? __fsub_rn(t, __fmul_rn(bk, roundf(__fdiv_rn(t, bk)))) : t;
 }
 
+// minimum image with the reciprocal box length (mixed form: the costs and the
+// neighbour lists of a pair use this same function throughout)
+__device__ __forceinline__ float min_image_rcp(float t, float bk, float rk) {
+    return bk != 0.f ? __fsub_rn(t, __fmul_rn(bk, rintf(__fmul_rn(t, rk)))) : t;
+}
+
+__device__ __forceinline__ float d2_f4_box_rcp(const float4 p, const float4 q, const float *bx,
+                                               const float *rx) {
+    const float dx = min_image_rcp(__fsub_rn(p.x, q.x), bx[0], rx[0]);
+    const float dy = min_image_rcp(__fsub_rn(p.y, q.y), bx[1], rx[1]);
+    const float dz = min_image_rcp(__fsub_rn(p.z, q.z), bx[2], rx[2]);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
 __device__ __forceinline__ float d2_f4_box(const float4 p, const float4 q, const float *bx) {
     const float dx = min_image_f(__fsub_rn(p.x, q.x), bx[0]);
     const float dy = min_image_f(__fsub_rn(p.y, q.y), bx[1]);
@@ -106,9 +120,9 @@ struct CostStored {      // costs kept in a row-major table of width m
 template <typename CT, bool BOX>
 struct CostF32 {         // costs recomputed from FP32 coordinates (minimum image when BOX)
     const float4 *b, *a;
-    float bx[3];
+    float bx[3], rx[3];  // box lengths and their reciprocals (0 for no wrap)
     __device__ __forceinline__ float d2(int i, int j) const {
-        if constexpr (BOX) return d2_f4_box(b[i], a[j], bx);
+        if constexpr (BOX) return d2_f4_box_rcp(b[i], a[j], bx, rx);
         else return d2_f4(b[i], a[j]);
     }
     __device__ __forceinline__ long long operator()(int i, int, int j) const {
@@ -499,6 +513,51 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
     }
 }
 
+// The m nearest columns of one row (mixed form): the m smallest squared
+// distances dist(j), j < ns (m < ns), as column indices in increasing order;
+// ties at the m-th value go to the lowest indices.  The whole warp works on
+// the row: the distances go to the scratch d (ns floats), the m-th smallest
+// is found by bisection on their bit patterns (non-negative floats order like
+// their bits) with warp-wide counts, and the chosen columns are compacted in
+// column order.  It picks the same set as the PAIRDISTS heap whenever the
+// m-th and (m+1)-th distances differ; the order within the row only decides
+// between tied optimal assignments.  The bisection stops as soon as a
+// threshold has exactly m distances below it.
+template <typename KT, typename DF>
+__device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, const DF &dist) {
+    const int lane = threadIdx.x & 31;
+    const unsigned ltmask = (1u << lane) - 1u;
+    for (int j = lane; j < ns; j += 32) d[j] = dist(j);
+    __syncwarp();
+    unsigned v = 0;   // grows to the m-th smallest bit pattern
+    bool exact = false;
+    for (int b = 30; b >= 0; --b) {
+        const unsigned t = v | (1u << b);
+        int c = 0;
+        for (int j = lane; j < ns; j += 32) c += __float_as_uint(d[j]) < t;
+        c = (int)__reduce_add_sync(kFull, (unsigned)c);
+        if (c <= m) v = t;
+        if (c == m) { exact = true; break; }   // {d < t} holds exactly m columns
+    }
+    int need_eq = 0, out = 0;
+    if (!exact) {   // v is the m-th smallest: take the ties at v lowest index first
+        int below = 0;
+        for (int j = lane; j < ns; j += 32) below += __float_as_uint(d[j]) < v;
+        need_eq = m - (int)__reduce_add_sync(kFull, (unsigned)below);
+    }
+    for (int b0 = 0; b0 < ns; b0 += 32) {
+        const int j = b0 + lane;
+        const unsigned u = j < ns ? __float_as_uint(d[j]) : 0xffffffffu;
+        const unsigned em = __ballot_sync(kFull, u == v);
+        const bool sel = u < v || (u == v && __popc(em & ltmask) < need_eq);
+        const unsigned sm = __ballot_sync(kFull, sel);
+        if (sel) krow[out + __popc(sm & ltmask)] = (KT)j;
+        out += __popc(sm);
+        need_eq -= min(need_eq, __popc(em));
+    }
+    __syncwarp();
+}
+
 // Coordinates of one permutation group as the assignment sees them: rows are
 // atoms of the fixed structure, columns atoms of the moved one.
 struct GroupCoords {
@@ -508,7 +567,7 @@ struct GroupCoords {
     const float4 *B4, *A4;   // FP32 copies (mixed form)
     int bulk;
     double box[3];
-    float bxf[3];
+    float bxf[3], rxf[3];    // FP32 box lengths and reciprocals (0: no wrap)
     // fixed-structure atom i as ITERATIVEALIGN holds it (centred for clusters)
     __device__ __forceinline__ void b(int i, double *o) const {
         for (int k = 0; k < 3; ++k) o[k] = xb[3 * i + k] - cmb[k];
@@ -531,14 +590,20 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
     if constexpr (RECOMP) {
         auto run = [&](const auto &cf) {
             if (!dense) {
-                float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
-                for (int i = lane; i < ns; i += 32)
-                    nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
+                if (ns <= kHeapMaxRow) {   // a heap per lane, one row each
+                    float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
+                    for (int i = lane; i < ns; i += 32)
+                        nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
+                } else {                   // the warp on one row at a time
+                    float *dr = (float *)(lb + L.lap_heap);
+                    for (int i = 0; i < ns; ++i)
+                        nearest_warp<KT>(kk + i * m, dr, ns, m, [&](int j) { return cf.d2(i, j); });
+                }
             }
             __syncwarp();
             return jv_warp<!kF32, KT>(ns, m, dense, cf, kk, v, dd, x, y, lab, fr, todo, ok);
         };
-        return run(CostF32<CT, BOX>{G.B4, G.A4, {G.bxf[0], G.bxf[1], G.bxf[2]}});
+        return run(CostF32<CT, BOX>{G.B4, G.A4, {G.bxf[0], G.bxf[1], G.bxf[2]}, {G.rxf[0], G.rxf[1], G.rxf[2]}});
     } else {
         CT *cc = (CT *)(lb + L.lap_cc);
         // squared distance of row i (bi: its FP64 coordinates) and column j
@@ -669,6 +734,7 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
         ca[k] = cs[k] / n;
         GC.box[k] = box[k];
         GC.bxf[k] = (float)box[k];
+        GC.rxf[k] = box[k] != 0.0 ? (float)(1.0 / box[k]) : 0.f;
     }
     // starting moved structure A0 (centred for clusters)
     auto a_start = [&](int j, double *out) {

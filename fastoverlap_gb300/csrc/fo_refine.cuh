@@ -11,7 +11,12 @@ struct RefLayout {
     int kkbytes;   // bytes per neighbour-list column index
 };
 
-constexpr int kHeapStride = 61;   // floats per lane of the neighbour-heap scratch (odd: no bank conflicts)
+// Neighbour lists of groups with more than 60 atoms (mixed form): rows of at
+// most kHeapMaxRow columns are selected by a heap per lane (kHeapStride floats
+// of scratch per lane, odd against bank conflicts), longer rows by the whole
+// warp on one row at a time (one row of distances as scratch).
+constexpr int kHeapMaxRow = 256;
+constexpr int kHeapStride = 61;
 
 __host__ __device__ inline size_t ref_a16(size_t b) { return (b + 15) & ~(size_t)15; }
 
@@ -22,8 +27,8 @@ __host__ __device__ inline int ref_kkbytes(int maxg) { return maxg <= 256 ? 1 : 
 // n atoms, largest permutation group maxg, FP32 coordinate copies (float4
 // per atom) when fp32, ctsize = bytes per integer cost (4 or 8), recomp =
 // costs recomputed from the FP32 coordinates instead of stored (only the
-// neighbour lists of groups with more than 60 atoms are kept, built through
-// a per-lane heap scratch).  The FP64 coordinates are not held here: the
+// neighbour lists of groups with more than 60 atoms are kept, selected
+// through a per-lane heap or one-row distance scratch).  The FP64 coordinates are not held here: the
 // refinement keeps them in global memory.
 __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsize, bool recomp,
                                            RefLayout &L) {
@@ -48,10 +53,15 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     L.lap_fr = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_todo = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_ok = p; p += ref_a16((size_t)maxg);
-    // the neighbour-heap scratch is only used before a group's assignment
-    // starts, so it overlays the assignment arrays
+    // the neighbour-selection scratch is only used before a group's
+    // assignment starts, so it overlays the assignment arrays
     L.lap_heap = L.lap_v;
-    const size_t heap_end = L.lap_v + ((recomp && sparse) ? ref_a16(4 * 32 * (size_t)kHeapStride) : 0);
+    size_t scratch = 0;
+    if (recomp && sparse) {
+        const size_t heap = 4 * 32 * (size_t)kHeapStride, row = 4 * (size_t)maxg;
+        scratch = ref_a16(heap > row ? heap : row);   // groups up to maxg use either
+    }
+    const size_t heap_end = L.lap_v + scratch;
     L.lap_end = p > heap_end ? p : heap_end;
 }
 
