@@ -11,7 +11,9 @@ pass of the whole alignment pipeline over the batch.
   e2e   : the same batch through fo_cluster_align_batch with host buffers
           (upload, pipeline, download), wall time.
   config: also reports the plain FP64 GPU form (batched and one pair per
-          call), and the error of the mixed form against FP64.
+          call), the error of the mixed form against FP64, and a served
+          stream (config.serving): Poisson arrivals (70% spherical N 13..500,
+          30% periodic N 64..1024) through fo_server_* with p50/p99 latency.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--npairs P] [--precision mixed|fp64]
@@ -67,6 +69,68 @@ def make_workload(npairs, seed_offset=0):
     except Exception:
         pass
     return pairs
+
+
+def _c4_pool(nproc):
+    cache = "/tmp/fo_bench_c4_pool.npz"
+    if os.path.exists(cache):
+        z = np.load(cache, allow_pickle=True)
+        return list(z["bases"])
+    from fastoverlap_gb300 import synth
+    ctxm = mp.get_context("spawn")
+    with ctxm.Pool(nproc) as pool:
+        bases = synth.config4_pool(pool=pool)
+    try:
+        np.savez(cache, bases=np.array(bases, dtype=object))
+    except Exception:
+        pass
+    return bases
+
+
+def serve_run(rate, duration, precision):
+    """Served stream: requests submitted at their Poisson arrival times from one
+    host thread; returns latency percentiles (submit -> complete) and the
+    completed requests per second of wall time."""
+    from fastoverlap_gb300 import synth
+    from fastoverlap_gb300.serve import Server
+    bases = _c4_pool(min(16, os.cpu_count() or 1))
+    reqs = list(synth.config4_requests(bases, rate=rate, duration=duration))
+    srv = Server(precision=precision)
+    # warm the kernels and the block pool with a few requests of each kind
+    for _, q in reqs[:32]:
+        _submit_req(srv, q)
+    srv.close()
+    srv = Server(precision=precision)
+    tickets = []
+    t0 = time.time()
+    for ta, q in reqs:
+        dt = t0 + ta - time.time()
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(_submit_req(srv, q))
+    t_sub = time.time() - t0
+    for t in tickets:
+        srv.wait(t)
+    wall = time.time() - t0
+    st = srv.stats()
+    srv.close()
+    ncl = sum(1 for _, q in reqs if q["kind"] == "cluster")
+    return {"arrival_rate_per_s": rate, "duration_s": duration, "requests": len(reqs),
+            "spherical": ncl, "periodic": len(reqs) - ncl, "submit_s": t_sub, "wall_s": wall,
+            "completed_per_s": st["completed"] / wall, "failed": int(st["failed"]),
+            "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
+            "latency_max_ms": st["latency_max_ms"], "batches": int(st["batches"]),
+            "mean_batch": st["mean_batch"],
+            "stand_in": "requests drawn from 48 spherical + 16 periodic seeded base structures, "
+                        "each with a fresh rotation/translation, permutation and noise"}
+
+
+def _submit_req(srv, q):
+    if q["kind"] == "cluster":
+        return srv.submit_cluster(q["pos1"], q["pos2"], q["perm"], Jmax=q["Jmax"], scale=q["sigma"],
+                                  nrot=q["nrot"])
+    return srv.submit_periodic(q["pos1"], q["pos2"], q["box"], q["perm"], scale=q["sigma"],
+                               nwave=q["nwave"], ndisps=q["ndisps"])
 
 
 class ClockSampler(object):
@@ -217,6 +281,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-duration", type=float, default=5.0, help="0 skips the served stream")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -340,6 +406,12 @@ def main():
             "kernel_ms_per_launch": top_ms,
             "kernel_share": kern[top][0] / sum(v[0] for v in kern.values())}
     launches = batch.plan_launches() * args.steps
+
+    if args.serve_duration > 0:
+        try:
+            cfg_extra["serving"] = serve_run(args.serve_rate, args.serve_duration, args.precision)
+        except Exception as e:   # reported, never required
+            cfg_extra["serving"] = {"error": str(e)}
 
     cpu = None
     if not args.no_cpu_baseline:

@@ -66,7 +66,8 @@ class FoRequest(ctypes.Structure):
 
 class FoServerOpts(ctypes.Structure):
     _fields_ = [("max_batch", ctypes.c_int), ("max_queue", ctypes.c_int),
-                ("max_wait_ms", ctypes.c_double)]
+                ("max_wait_ms", ctypes.c_double), ("workers", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
 
 
 class FoServerStats(ctypes.Structure):

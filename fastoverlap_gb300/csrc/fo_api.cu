@@ -1154,3 +1154,10 @@ void fo_profile_reset(fo_ctx *ctx) {
 }
 
 }  // extern "C"
+
+// library-internal (not in the public header): the server's worker contexts
+namespace fo {
+fo_opts ctx_opts(const fo_ctx *ctx) { return ctx->opts; }
+void ctx_set_budget(fo_ctx *ctx, size_t bytes) { ctx->opts.hbm_budget_bytes = bytes; }
+}  // namespace fo
+

@@ -179,10 +179,12 @@ void launch_bulk_fft(const BulkBuffers &b, bool fp32, cudaStream_t s) {
     for (int axis = 0; axis < 3; ++axis) {
         if (fp32) {
             size_t sm = sizeof(float2) * (2 * kLines * b.maxM + b.maxM);
+            allow_max_smem<k_bulk_fft_axis<float, float2>>();
             k_bulk_fft_axis<float, float2><<<grid, 256, sm, s>>>(b.pairs, (float2 *)b.fgrid,
                                                                 (float *)b.grid, axis, axis == 2);
         } else {
             size_t sm = sizeof(double2) * (2 * kLines * b.maxM + b.maxM);
+            allow_max_smem<k_bulk_fft_axis<double, double2>>();
             k_bulk_fft_axis<double, double2><<<grid, 256, sm, s>>>(b.pairs, (double2 *)b.fgrid,
                                                                   (double *)b.grid, axis, axis == 2);
         }

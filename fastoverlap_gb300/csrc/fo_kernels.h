@@ -3,9 +3,30 @@
 // given stream.
 #pragma once
 #include <cuda_runtime.h>
+#include <mutex>
+#include "../../include/fastoverlap_gb300.h"
 #include "fo_common.cuh"
 
 namespace fo {
+
+// Raise kernel K's dynamic shared-memory limit to the device's opt-in maximum,
+// once per kernel.  The limit is a process-wide attribute of the kernel: a
+// thread that lowered it for a small launch would make another thread's
+// larger launch of the same kernel fail, so it is only ever set to the
+// maximum (the launch's own size still decides occupancy).  Set on the device
+// current at the first launch.
+template <auto K>
+inline void allow_max_smem() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, K);
+        cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    });
+}
 
 struct SphBuffers {
     const PairDev *pairs;
@@ -86,5 +107,9 @@ void launch_findpeaks_from(const PairDev *pairs, int npairs, void *grid, double 
 void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,
                    cudaEvent_t fork, cudaEvent_t *join);
 void launch_select(const RefineBuffers &b, cudaStream_t s);
+
+// context options (library-internal; the server creates worker contexts)
+fo_opts ctx_opts(const fo_ctx *ctx);
+void ctx_set_budget(fo_ctx *ctx, size_t bytes);
 
 }  // namespace fo

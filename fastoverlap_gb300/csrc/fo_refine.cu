@@ -110,8 +110,10 @@ __device__ __forceinline__ CT cost_of_f32(float d2) {
 }
 
 // Cost of row i, scan position t, column j.
+// kByColumn: the cost depends on the column only, not on its scan position.
 template <typename CT>
 struct CostStored {      // costs kept in a row-major table of width m
+    static constexpr bool kByColumn = false;
     const CT *cc;
     int m;
     __device__ __forceinline__ long long operator()(int i, int t, int) const { return (long long)cc[i * m + t]; }
@@ -119,6 +121,7 @@ struct CostStored {      // costs kept in a row-major table of width m
 
 template <typename CT, bool BOX>
 struct CostF32 {         // costs recomputed from FP32 coordinates (minimum image when BOX)
+    static constexpr bool kByColumn = true;
     const float4 *b, *a;
     float bx[3], rx[3];  // box lengths and their reciprocals (0 for no wrap)
     __device__ __forceinline__ float d2(int i, int j) const {
@@ -346,14 +349,19 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
             __syncwarp();
             if (lane == 0) todo[td] = jc;
             --td;
-            int tpos = -1;
-            for (int q = 0; q < 2; ++q) {
-                int t = lane + 32 * q;
-                bool hit = (t < m) && COL(i, t) == jc;
-                unsigned hm = __ballot_sync(kFull, hit);
-                if (hm && tpos < 0) tpos = 32 * q + __ffs(hm) - 1;
+            // scan position of jc in row i: jc is the column row i holds, and
+            // rows only ever hold columns of their own list
+            int tpos = jc;
+            if (!CF::kByColumn && !dense) {
+                tpos = -1;
+                for (int q = 0; q < 2; ++q) {
+                    int t = lane + 32 * q;
+                    bool hit = (t < m) && COL(i, t) == jc;
+                    unsigned hm = __ballot_sync(kFull, hit);
+                    if (hm && tpos < 0) tpos = 32 * q + __ffs(hm) - 1;
+                }
+                if (tpos < 0) return 5;
             }
-            if (tpos < 0) return 5;
             const long long hh = cost(i, tpos, jc) - v[jc] - mn;
             bool eq[2];
             int jq[2];
@@ -523,31 +531,53 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
 // m-th and (m+1)-th distances differ; the order within the row only decides
 // between tied optimal assignments.  The bisection stops as soon as a
 // threshold has exactly m distances below it.
+// Rows of up to 32*kNearReg columns keep their distances in registers.
+constexpr int kNearReg = 16;
+
 template <typename KT, typename DF>
 __device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, const DF &dist) {
     const int lane = threadIdx.x & 31;
     const unsigned ltmask = (1u << lane) - 1u;
-    for (int j = lane; j < ns; j += 32) d[j] = dist(j);
+    const bool inreg = ns <= 32 * kNearReg;
+    unsigned r[kNearReg];   // bit patterns of columns lane + 32k (all ones beyond ns)
+#pragma unroll
+    for (int k = 0; k < kNearReg; ++k) {
+        const int j = lane + 32 * k;
+        r[k] = (inreg && j < ns) ? __float_as_uint(dist(j)) : 0xffffffffu;
+    }
+    if (!inreg)
+        for (int j = lane; j < ns; j += 32) d[j] = dist(j);
     __syncwarp();
+    auto count_below = [&](unsigned t) -> int {
+        int c = 0;
+        if (inreg) {
+#pragma unroll
+            for (int k = 0; k < kNearReg; ++k) c += r[k] < t;
+        } else {
+            for (int j = lane; j < ns; j += 32) c += __float_as_uint(d[j]) < t;
+        }
+        return (int)__reduce_add_sync(kFull, (unsigned)c);
+    };
     unsigned v = 0;   // grows to the m-th smallest bit pattern
     bool exact = false;
     for (int b = 30; b >= 0; --b) {
         const unsigned t = v | (1u << b);
-        int c = 0;
-        for (int j = lane; j < ns; j += 32) c += __float_as_uint(d[j]) < t;
-        c = (int)__reduce_add_sync(kFull, (unsigned)c);
+        const int c = count_below(t);
         if (c <= m) v = t;
         if (c == m) { exact = true; break; }   // {d < t} holds exactly m columns
     }
     int need_eq = 0, out = 0;
-    if (!exact) {   // v is the m-th smallest: take the ties at v lowest index first
-        int below = 0;
-        for (int j = lane; j < ns; j += 32) below += __float_as_uint(d[j]) < v;
-        need_eq = m - (int)__reduce_add_sync(kFull, (unsigned)below);
-    }
+    if (!exact) need_eq = m - count_below(v);   // v is the m-th smallest: ties at v, lowest index first
     for (int b0 = 0; b0 < ns; b0 += 32) {
         const int j = b0 + lane;
-        const unsigned u = j < ns ? __float_as_uint(d[j]) : 0xffffffffu;
+        unsigned u = 0xffffffffu;
+        if (inreg) {
+#pragma unroll
+            for (int k = 0; k < kNearReg; ++k)
+                if (b0 == 32 * k) u = r[k];
+        } else if (j < ns) {
+            u = __float_as_uint(d[j]);
+        }
         const unsigned em = __ballot_sync(kFull, u == v);
         const bool sel = u < v || (u == v && __popc(em & ltmask) < need_eq);
         const unsigned sm = __ballot_sync(kFull, sel);
@@ -1013,8 +1043,7 @@ void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux,
         cudaStream_t s = naux ? aux[k % naux] : main;
 #define FO_LAUNCH_REFINE(DT, CT, RC, BX)                                                              \
     do {                                                                                              \
-        cudaFuncSetAttribute(k_refine_warp<DT, CT, RC, BX>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             (int)bk.smem);                                                           \
+        allow_max_smem<k_refine_warp<DT, CT, RC, BX>>();                                             \
         k_refine_warp<DT, CT, RC, BX><<<bk.count, 32, bk.smem, s>>>(                                  \
             b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,      \
             b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);                                       \

@@ -1,16 +1,20 @@
 // fo_server.cu -- serving: alignment requests admitted as they arrive.
 //
 // Host code over the public C ABI.  Requests are copied into the server at
-// submission (validated first, so a bad request never reaches a batch).  One
-// worker thread owns the context: whenever the GPU is free it takes the
-// pending requests in arrival order (continuous batching, at most max_batch),
-// splits them by kind, and runs each kind as one resident plan (upload, the
-// whole pipeline, download).  Device memory comes from the context's block
-// pool, so a steady stream allocates nothing.  A plan larger than the HBM
-// budget is split in halves until it fits; a request that does not fit alone
-// completes with FO_ERR_OOM_BUDGET.  Latency is measured from submission to
-// completion on the host's steady clock.
+// submission (validated first, so a bad request never reaches a batch).
+// Several worker threads each own a context (the caller's and contexts
+// created with its options), so their plans run on separate streams: the
+// long tail of one batch -- a few large pairs still refining -- overlaps the
+// next batch.  A free worker takes the pending requests in arrival order
+// (continuous batching, at most max_batch), splits them by kind, and runs each
+// kind as one resident plan (upload, the whole pipeline, download).  Device
+// memory comes from each context's block pool, so a steady stream allocates
+// nothing.  The HBM budget is shared evenly by the workers; a plan larger than
+// a worker's share is split in halves until it fits, and a request that does
+// not fit alone completes with FO_ERR_OOM_BUDGET.  Latency is measured from
+// submission to completion on the host's steady clock.
 #include "../../include/fastoverlap_gb300.h"
+#include "fo_kernels.h"
 
 #include <algorithm>
 #include <chrono>
@@ -74,29 +78,31 @@ fo_status validate(const fo_request &q) {
 }  // namespace
 
 struct fo_server {
-    fo_ctx *ctx = nullptr;
+    fo_ctx *user_ctx = nullptr;
+    size_t user_budget = 0;
+    std::vector<fo_ctx *> ctxs;   // one per worker; ctxs[0] is the caller's
     fo_server_opts o{};
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<ReqP> pending;
     std::unordered_map<int64_t, ReqP> finished;
-    int64_t next_ticket = 1, inflight = 0;
+    int64_t next_ticket = 1;
     bool stop = false;
-    std::thread worker;
+    std::vector<std::thread> workers;
     // statistics
     int64_t n_sub = 0, n_done = 0, n_fail = 0, n_batches = 0, n_batched = 0;
     std::vector<double> lat_ms;
     double busy_ms = 0;
 
-    void run_kind(std::vector<Req *> &rs, int kind);
-    void run_group(Req **rs, int n, int kind);
-    void loop();
+    void run_kind(fo_ctx *ctx, std::vector<Req *> &rs, int kind);
+    void run_group(fo_ctx *ctx, Req **rs, int n, int kind);
+    void loop(fo_ctx *ctx);
 };
 
 // One plan for n requests of one kind; halves on FO_ERR_OOM_BUDGET, and runs
 // requests one by one when a plan is refused for a reason the submit-time
 // checks did not catch (so that only the offending request fails).
-void fo_server::run_group(Req **rs, int n, int kind) {
+void fo_server::run_group(fo_ctx *ctx, Req **rs, int n, int kind) {
     if (n <= 0) return;
     std::vector<double> p1, p2;
     std::vector<int> perm, gsz;
@@ -145,10 +151,10 @@ void fo_server::run_group(Req **rs, int n, int kind) {
     if (s != FO_OK) {
         if (n > 1) {
             if (s == FO_ERR_OOM_BUDGET) {
-                run_group(rs, n / 2, kind);
-                run_group(rs + n / 2, n - n / 2, kind);
+                run_group(ctx, rs, n / 2, kind);
+                run_group(ctx, rs + n / 2, n - n / 2, kind);
             } else {
-                for (int i = 0; i < n; ++i) run_group(rs + i, 1, kind);
+                for (int i = 0; i < n; ++i) run_group(ctx, rs + i, 1, kind);
             }
         } else {
             rs[0]->status = s;
@@ -180,14 +186,14 @@ void fo_server::run_group(Req **rs, int n, int kind) {
     }
 }
 
-void fo_server::run_kind(std::vector<Req *> &rs, int kind) {
+void fo_server::run_kind(fo_ctx *ctx, std::vector<Req *> &rs, int kind) {
     std::vector<Req *> sel;
     for (Req *r : rs)
         if (r->r.kind == kind) sel.push_back(r);
-    run_group(sel.data(), (int)sel.size(), kind);
+    run_group(ctx, sel.data(), (int)sel.size(), kind);
 }
 
-void fo_server::loop() {
+void fo_server::loop(fo_ctx *ctx) {
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
         cv_work.wait(lk, [&] { return stop || !pending.empty(); });
@@ -200,13 +206,12 @@ void fo_server::loop() {
             batch.push_back(std::move(pending.front()));
             pending.pop_front();
         }
-        inflight = (int64_t)batch.size();
         lk.unlock();
         const Clock::time_point t0 = Clock::now();
         std::vector<Req *> rs;
         for (auto &b : batch) rs.push_back(b.get());
-        run_kind(rs, FO_KIND_CLUSTER);
-        run_kind(rs, FO_KIND_BULK);
+        run_kind(ctx, rs, FO_KIND_CLUSTER);
+        run_kind(ctx, rs, FO_KIND_BULK);
         const Clock::time_point t1 = Clock::now();
         lk.lock();
         busy_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
@@ -219,7 +224,6 @@ void fo_server::loop() {
             const int64_t t = b->ticket;
             finished[t] = std::move(b);
         }
-        inflight = 0;
         cv_done.notify_all();
     }
 }
@@ -228,13 +232,30 @@ extern "C" {
 
 fo_status fo_server_create(fo_ctx *ctx, const fo_server_opts *opts, fo_server **out) {
     if (!ctx || !out) return FO_ERR_BAD_ARGS;
+    *out = nullptr;
     fo_server *s = new fo_server();
-    s->ctx = ctx;
     if (opts) s->o = *opts;
     if (s->o.max_batch <= 0) s->o.max_batch = 4096;
     if (s->o.max_queue <= 0) s->o.max_queue = 1 << 20;
     if (s->o.max_wait_ms < 0) s->o.max_wait_ms = 0;
-    s->worker = std::thread([s] { s->loop(); });
+    if (s->o.workers <= 0) s->o.workers = 2;
+    fo_opts co = fo::ctx_opts(ctx);
+    s->user_ctx = ctx;
+    s->user_budget = co.hbm_budget_bytes;
+    const size_t share = co.hbm_budget_bytes / (size_t)s->o.workers;
+    if (co.hbm_budget_bytes) co.hbm_budget_bytes = share ? share : 1;
+    s->ctxs.push_back(ctx);
+    for (int w = 1; w < s->o.workers; ++w) {
+        fo_ctx *c = nullptr;
+        if (fo_ctx_create(&co, &c) != FO_OK) {
+            for (size_t k = 1; k < s->ctxs.size(); ++k) fo_ctx_destroy(s->ctxs[k]);
+            delete s;
+            return FO_ERR_CUDA;
+        }
+        s->ctxs.push_back(c);
+    }
+    for (fo_ctx *c : s->ctxs) fo::ctx_set_budget(c, co.hbm_budget_bytes);
+    for (fo_ctx *c : s->ctxs) s->workers.emplace_back([s, c] { s->loop(c); });
     *out = s;
     return FO_OK;
 }
@@ -333,7 +354,10 @@ void fo_server_destroy(fo_server *srv) {
         srv->stop = true;
     }
     srv->cv_work.notify_all();
-    if (srv->worker.joinable()) srv->worker.join();
+    for (auto &w : srv->workers)
+        if (w.joinable()) w.join();
+    for (size_t k = 1; k < srv->ctxs.size(); ++k) fo_ctx_destroy(srv->ctxs[k]);
+    fo::ctx_set_budget(srv->user_ctx, srv->user_budget);   // the caller's context as it was
     delete srv;
 }
 

@@ -481,13 +481,13 @@ void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s) {
     dim3 grid(b.maxL + 1, b.npairs);
     if (fp32) {
         size_t sm = sizeof(float2) * (kMaxWM * kTB + kMaxWM * kTA + kTA * kMaxWM) + sizeof(float) * kTB * kTA;
-        cudaFuncSetAttribute(k_sph_coeff<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        allow_max_smem<k_sph_coeff<float, float2>>();
         k_sph_coeff<float, float2><<<grid, 256, sm, s>>>(b.pairs, b.groups, (const float2 *)b.ylmA,
                                                         (const float2 *)b.ylmB, (const float *)b.W,
                                                         (float2 *)b.coef);
     } else {
         size_t sm = sizeof(double2) * (kMaxWM * kTB + kMaxWM * kTA + kTA * kMaxWM) + sizeof(double) * kTB * kTA;
-        cudaFuncSetAttribute(k_sph_coeff<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        allow_max_smem<k_sph_coeff<double, double2>>();
         k_sph_coeff<double, double2><<<grid, 256, sm, s>>>(b.pairs, b.groups, (const double2 *)b.ylmA,
                                                           (const double2 *)b.ylmB, (const double *)b.W,
                                                           (double2 *)b.coef);
@@ -498,12 +498,12 @@ void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s) {
     dim3 grid(b.maxG, b.npairs);
     if (fp32) {
         size_t sm = sizeof(float2) * (3 * b.maxG * b.maxG + b.maxG);
-        cudaFuncSetAttribute(k_isoft<float, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        allow_max_smem<k_isoft<float, float2>>();
         k_isoft<float, float2><<<grid, 256, sm, s>>>(b.pairs, (const float2 *)b.coef,
                                                     (const float *const *)b.dtab, (float *)b.grid);
     } else {
         size_t sm = sizeof(double2) * (3 * b.maxG * b.maxG + b.maxG);
-        cudaFuncSetAttribute(k_isoft<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        allow_max_smem<k_isoft<double, double2>>();
         k_isoft<double, double2><<<grid, 256, sm, s>>>(b.pairs, (const double2 *)b.coef,
                                                       (const double *const *)b.dtab, (double *)b.grid);
     }

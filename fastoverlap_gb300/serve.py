@@ -23,10 +23,10 @@ FO_KIND_BULK = 1
 
 class Server(object):
     def __init__(self, ctx=None, precision="mixed", max_batch=4096, max_queue=0, max_wait_ms=0.0,
-                 hbm_budget_bytes=0):
+                 hbm_budget_bytes=0, workers=2):
         self.ctx = ctx or _lib.Context(precision=precision, hbm_budget_bytes=hbm_budget_bytes)
         self.lib = self.ctx.lib
-        opts = _lib.FoServerOpts(int(max_batch), int(max_queue), float(max_wait_ms))
+        opts = _lib.FoServerOpts(int(max_batch), int(max_queue), float(max_wait_ms), int(workers), 0)
         h = ctypes.c_void_p()
         self.ctx.check(self.lib.fo_server_create(self.ctx.h, ctypes.byref(opts), ctypes.byref(h)),
                        "server create")

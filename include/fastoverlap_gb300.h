@@ -241,12 +241,15 @@ fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double bo
  * No counterpart in the reference (its classes align one pair per call).
  * Spherical (SphericalAlign) and periodic (PeriodicAlign) requests of any
  * size are submitted one at a time, from any host thread; inputs are copied
- * at submission.  A worker thread gathers every request pending when the GPU
- * is free (continuous batching, arrival order, at most max_batch), runs them
- * as one resident plan per kind on the context's stream, and completes their
- * tickets.  A plan larger than the context's HBM budget is split in halves;
- * a request that does not fit alone completes with FO_ERR_OOM_BUDGET.  The
- * server owns the context while it lives: make no other call on it.        */
+ * at submission.  `workers` worker threads (the given context and contexts
+ * created with its options, each on its own streams) take every request
+ * pending when they are free (continuous batching, arrival order, at most
+ * max_batch), run them as one resident plan per kind, and complete their
+ * tickets; one batch's last large pairs overlap the next batch.  The
+ * context's HBM budget is shared evenly by the workers: a plan larger than a
+ * share is split in halves, and a request that does not fit alone completes
+ * with FO_ERR_OOM_BUDGET.  The server owns the context while it lives: make
+ * no other call on it.                                                       */
 typedef struct fo_server fo_server;
 
 enum { FO_KIND_CLUSTER = 0, FO_KIND_BULK = 1 };
@@ -272,15 +275,17 @@ typedef struct {
 typedef struct {
     int    max_batch;     /* requests per plan; <= 0: 4096                         */
     int    max_queue;     /* pending requests before FO_ERR_QUEUE_FULL; <= 0: 1<<20 */
-    double max_wait_ms;   /* once the GPU is free, wait up to this long for more
+    double max_wait_ms;   /* once a worker is free, wait up to this long for more
                              requests before launching; 0: launch at once           */
+    int    workers;       /* concurrent batches (contexts); <= 0: 2                */
+    int    reserved;
 } fo_server_opts;
 
 typedef struct {
     int64_t submitted, completed, failed, batches;
     double  latency_p50_ms, latency_p99_ms, latency_max_ms;  /* submit -> complete */
     double  mean_batch;   /* requests per batch                                    */
-    double  busy_ms;      /* wall time with a batch being prepared or run           */
+    double  busy_ms;      /* summed over workers: time with a batch being prepared or run */
 } fo_server_stats;
 
 fo_status fo_server_create(fo_ctx *ctx, const fo_server_opts *opts, fo_server **out);
