@@ -3,9 +3,11 @@
 The library is the only compute path: if it cannot be loaded (not built, no
 CUDA device) every call raises; there is no CPU fallback.
 """
+import atexit
 import ctypes
 import os
 import threading
+import weakref
 
 import numpy as np
 
@@ -146,6 +148,25 @@ EXPORTS = {
 _LIB = None
 _LOCK = threading.Lock()
 
+# Library objects still open at interpreter exit are closed here, servers
+# first, then plans, then contexts, while the interpreter is intact: calling
+# into the library from __del__ during interpreter teardown is not safe.
+_LIVE = {"servers": weakref.WeakSet(), "plans": weakref.WeakSet(), "contexts": weakref.WeakSet()}
+
+
+def track(kind, obj):
+    _LIVE[kind].add(obj)
+
+
+@atexit.register
+def _close_all():
+    for kind in ("servers", "plans", "contexts"):
+        for obj in list(_LIVE[kind]):
+            try:
+                obj.close()
+            except Exception:
+                pass
+
 
 def load(build_if_missing=True):
     """Load the CUDA library (building it in place with nvcc if needed)."""
@@ -191,6 +212,7 @@ class Context(object):
         st = self.lib.fo_ctx_create(ctypes.byref(opts), ctypes.byref(h))
         if st != FO_OK:
             raise FoError(st, "fo_ctx_create (is a CUDA device visible?)")
+        track("contexts", self)
         self.h = h
         self.precision = precision
 

@@ -90,6 +90,7 @@ class _BatchBase(object):
                 ctypes.byref(h))
         self.ctx.check(st, "plan create")
         self.plan_h = h
+        _lib.track("plans", self)
         return self
 
     def plan_run(self):

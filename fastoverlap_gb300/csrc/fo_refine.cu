@@ -32,6 +32,11 @@
 
 #include <cstdint>
 
+// 1: the mixed form runs the augmenting row reduction too (as the FP64 form)
+#ifndef FO_MIXED_ARR
+#define FO_MIXED_ARR 0
+#endif
+
 namespace fo {
 
 constexpr unsigned kFull = 0xffffffffu;
@@ -631,7 +636,7 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                 }
             }
             __syncwarp();
-            return jv_warp<!kF32, KT>(ns, m, dense, cf, kk, v, dd, x, y, lab, fr, todo, ok);
+            return jv_warp<!kF32 || FO_MIXED_ARR, KT>(ns, m, dense, cf, kk, v, dd, x, y, lab, fr, todo, ok);
         };
         return run(CostF32<CT, BOX>{G.B4, G.A4, {G.bxf[0], G.bxf[1], G.bxf[2]}, {G.rxf[0], G.rxf[1], G.rxf[2]}});
     } else {

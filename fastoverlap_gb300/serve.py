@@ -32,6 +32,7 @@ class Server(object):
                        "server create")
         self.h = h
         self.natoms = {}
+        _lib.track("servers", self)
 
     # -- submission ---------------------------------------------------------------
     def _submit(self, req, pos1, pos2, perm):

@@ -105,3 +105,25 @@ def test_plan_runs_after_l2_flush_and_events(fo):
     assert np.array_equal(b.plan_results(False)["dist"], first)
     assert "refine" in ctx.profile()
     b.close()
+
+
+def test_exit_with_open_objects(fo):
+    """A process that exits with a server, a plan and contexts still open
+    exits cleanly (they are closed before the interpreter is torn down)."""
+    import subprocess
+    import sys
+    import os
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "import fastoverlap_gb300 as F\n"
+            "from fastoverlap_gb300 import synth\n"
+            "ps = synth.config2(4, seed_offset=31)\n"
+            "ctx = F.Context(precision='mixed')\n"
+            "b = F.ClusterBatch(ctx, [p['pos1'] for p in ps], [p['pos2'] for p in ps], [p['perm'] for p in ps],"
+            " Jmax=[p['Jmax'] for p in ps], scale=0.3).plan()\n"
+            "b.plan_run(); b.plan_wait()\n"
+            "srv = F.Server(precision='mixed')\n"
+            "t = srv.submit_cluster(ps[0]['pos1'], ps[0]['pos2'], ps[0]['perm'], Jmax=7)\n"
+            "print('ok', srv.wait(t)['status'])\n") % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "ok 0" in r.stdout
