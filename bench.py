@@ -11,7 +11,9 @@ pass of the whole alignment pipeline over the batch.
   e2e   : the same batch through fo_cluster_align_batch with host buffers
           (upload, pipeline, download), wall time.
   config: also reports the plain FP64 GPU form (batched and one pair per
-          call), the error of the mixed form against FP64, and a served
+          call), the error of the mixed form against FP64, the large-bandwidth
+          study (config.precision_study_c3: 64 pairs of 1000 atoms at Jmax 31,
+          FP64 against mixed), and a served
           stream (config.serving): Poisson arrivals (70% spherical N 13..500,
           30% periodic N 64..1024) through fo_server_* with p50/p99 latency.
 
@@ -69,6 +71,53 @@ def make_workload(npairs, seed_offset=0):
     except Exception:
         pass
     return pairs
+
+
+def _gen_c3(k):
+    from fastoverlap_gb300 import synth
+    p = synth.config3(1, seed_offset=k)[0]
+    return (p["pos1"], p["pos2"], [np.asarray(g) for g in p["perm"]])
+
+
+def c3_run(npairs):
+    """Large-bandwidth precision study (config 3): 1000-atom clusters (800:200),
+    Jmax 31, sigma 0.25, 20 peaks; the plain FP64 form against the mixed form."""
+    from fastoverlap_gb300 import ClusterBatch, Context
+    cache = "/tmp/fo_bench_c3_%d.npz" % npairs
+    if os.path.exists(cache):
+        pairs = list(np.load(cache, allow_pickle=True)["pairs"])
+    else:
+        with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+            pairs = pool.map(_gen_c3, range(npairs))
+        try:
+            np.savez(cache, pairs=np.array(pairs, dtype=object))
+        except Exception:
+            pass
+    out, res = {"pairs": npairs, "atoms": 1000, "jmax": 31, "peaks": 20}, {}
+    for prec in ("fp64", "mixed"):
+        ctx = Context(precision=prec)
+        b = ClusterBatch(ctx, [p[0] for p in pairs], [p[1] for p in pairs], [p[2] for p in pairs],
+                         Jmax=31, scale=0.25, nrot=20).plan()
+        b.plan_run()
+        b.plan_wait()
+        ctx.record(0)
+        b.plan_run()
+        ctx.record(1)
+        b.plan_wait()
+        ms = ctx.elapsed_ms(0, 1)
+        res[prec] = b.plan_results(with_coords=True)
+        out["%s_pairs_per_s" % prec] = npairs / (ms / 1000.0)
+        b.close()
+        ctx.close()
+    a, f = res["mixed"], res["fp64"]
+    ok = (a["status"] == 0) & (f["status"] == 0)
+    out["mixed_vs_fp64_max_rel_dist"] = float(np.max(np.abs(a["dist"][ok] - f["dist"][ok]) / f["dist"][ok]))
+    out["mixed_vs_fp64_identical_perm_frac"] = float(np.mean([np.array_equal(x, y) for x, y, o in
+                                                              zip(a["perm"], f["perm"], ok) if o]))
+    om_a, om_f = a["result"]["overlap_max"][ok], f["result"]["overlap_max"][ok]
+    out["mixed_vs_fp64_max_rel_overlap_max"] = float(np.max(np.abs(om_a - om_f) / np.abs(om_f)))
+    out["pairs_failed"] = int((~ok).sum())
+    return out
 
 
 def _c4_pool(nproc):
@@ -281,6 +330,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=32)
+    ap.add_argument("--c3-pairs", type=int, default=64, help="0 skips the large-bandwidth study")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-duration", type=float, default=5.0, help="0 skips the served stream")
     args = ap.parse_args()
@@ -416,6 +466,12 @@ def main():
             "kernel_ms_per_launch": top_ms,
             "kernel_share": kern[top][0] / sum(v[0] for v in kern.values())}
     launches = batch.plan_launches() * args.steps
+
+    if args.c3_pairs > 0:
+        try:
+            cfg_extra["precision_study_c3"] = c3_run(args.c3_pairs)
+        except Exception as e:   # reported, never required
+            cfg_extra["precision_study_c3"] = {"error": str(e)}
 
     if args.serve_duration > 0:
         try:
