@@ -136,7 +136,7 @@ def _c4_pool(nproc):
     return bases
 
 
-def serve_run(rate, duration, precision):
+def serve_run(rate, duration, precision, workers=2):
     """Served stream: requests submitted at their Poisson arrival times from one
     host thread; returns latency percentiles (submit -> complete) and the
     completed requests per second of wall time."""
@@ -144,12 +144,12 @@ def serve_run(rate, duration, precision):
     from fastoverlap_gb300.serve import Server
     bases = _c4_pool(min(16, os.cpu_count() or 1))
     reqs = list(synth.config4_requests(bases, rate=rate, duration=duration))
-    srv = Server(precision=precision)
+    srv = Server(precision=precision, workers=workers)
     # warm the kernels and the block pool with a few requests of each kind
     for _, q in reqs[:32]:
         _submit_req(srv, q)
     srv.close()
-    srv = Server(precision=precision)
+    srv = Server(precision=precision, workers=workers)
     tickets = []
     t0 = time.time()
     for ta, q in reqs:
@@ -166,7 +166,7 @@ def serve_run(rate, duration, precision):
     ncl = sum(1 for _, q in reqs if q["kind"] == "cluster")
     return {"arrival_rate_per_s": rate, "duration_s": duration, "requests": len(reqs),
             "spherical": ncl, "periodic": len(reqs) - ncl, "submit_s": t_sub, "wall_s": wall,
-            "completed_per_s": st["completed"] / wall, "failed": int(st["failed"]),
+            "workers": workers, "completed_per_s": st["completed"] / wall, "failed": int(st["failed"]),
             "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
             "latency_max_ms": st["latency_max_ms"], "batches": int(st["batches"]),
             "mean_batch": st["mean_batch"],
