@@ -481,6 +481,304 @@ __device__ __forceinline__ DT pdist2(const DT *c1, const DT *c2, int bulk, const
     return d;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 building blocks of the mixed form.  GB300 issues FP64 at a small
+// fraction of its FP32 rate, and one warp-wide FP64 instruction costs the
+// same with one lane active as with 32, so the mixed form counts FP64
+// instructions rather than lanes: small matrix work runs one entry per lane,
+// sums over the warp are halved level by level, and the eigen-solve iterates
+// in FP32 with one FP64 correction.
+
+template <int N>
+__host__ __device__ constexpr unsigned long long pack_nibbles(const int (&a)[N]) {
+    unsigned long long r = 0;
+    for (int i = 0; i < N; ++i) r |= (unsigned long long)(a[i] & 15) << (4 * i);
+    return r;
+}
+template <int N>
+__host__ __device__ constexpr unsigned pack_flags(const int (&a)[N]) {
+    unsigned r = 0;
+    for (int i = 0; i < N; ++i) r |= (a[i] ? 1u : 0u) << i;
+    return r;
+}
+__device__ __forceinline__ int nibble(unsigned long long t, int i) { return (int)((t >> (4 * i)) & 15); }
+__device__ __forceinline__ bool flag(unsigned t, int i) { return (t >> i) & 1u; }
+
+// x or -x, by the sign bit (an integer instruction).
+__device__ __forceinline__ double flip_sign(double x, bool s) {
+    return __hiloint2double(__double2hiint(x) ^ (s ? (int)0x80000000 : 0), __double2loint(x));
+}
+
+// Warp sum of M doubles per lane by recursive halving: at each butterfly
+// level a lane keeps half of its values and adds its partner's copy of that
+// half, ceil(M/2) + ceil(M/4) + ... additions in all instead of 5M.  Value k's
+// total ends in v[0] of lane halve_lane(k, M) (and of the lanes that differ
+// from it only in levels where one value was left).
+__host__ __device__ constexpr int halve_lane(int k, int m) {
+    int lane = 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        if (m == 1) continue;
+        const int h = (m + 1) / 2;
+        if (k >= h) { lane |= o; k -= h; }
+        m = h;
+    }
+    return lane;
+}
+template <int M, int O = 16>
+__device__ __forceinline__ void warp_halve(double *v, int lane) {
+    if constexpr (O > 0) {
+        if constexpr (M == 1) {
+            v[0] += __shfl_xor_sync(kFull, v[0], O);
+            warp_halve<1, O / 2>(v, lane);
+        } else {
+            constexpr int H = (M + 1) / 2;
+            const bool up = (lane & O) != 0;
+#pragma unroll
+            for (int i = 0; i < H; ++i) {
+                const double lo = v[i], hi = (H + i < M) ? v[H + i] : 0.0;
+                v[i] = (up ? hi : lo) + __shfl_xor_sync(kFull, up ? lo : hi, O);
+            }
+            warp_halve<H, O / 2>(v, lane);
+        }
+    }
+}
+
+// Cyclic Jacobi rotations (Golub & Van Loan 8.5) on a symmetric 4x4 FP32
+// matrix scaled to unit largest element; a sweep in which every off-diagonal
+// element is at most 2^-22 ends it.  Columns of V are the eigenvectors.
+__device__ __forceinline__ void jacobi4f(float (&a)[4][4], float (&V)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.f : 0.f;
+    for (int sweep = 0; sweep < 16; ++sweep) {
+        bool rotated = false;
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int r = p + 1; r < 4; ++r) {
+                const float apr = a[p][r];
+                if (fabsf(apr) <= 2.384185791015625e-7f) continue;
+                rotated = true;
+                const float theta = (a[r][r] - a[p][p]) / (2.f * apr);
+                const float t = copysignf(1.f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
+                const float c = 1.f / sqrtf(fmaf(t, t, 1.f)), s = t * c;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float akp = a[k][p], akr = a[k][r];
+                    a[k][p] = c * akp - s * akr;
+                    a[k][r] = s * akp + c * akr;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float apk = a[p][k], ark = a[r][k];
+                    a[p][k] = c * apk - s * ark;
+                    a[r][k] = s * apk + c * ark;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float vkp = V[k][p], vkr = V[k][r];
+                    V[k][p] = c * vkp - s * vkr;
+                    V[k][r] = s * vkp + c * vkr;
+                }
+            }
+        if (!rotated) break;
+    }
+}
+
+// Horn's matrix (J. Opt. Soc. Am. A 4, 629 (1987)) of H = sum_j a_j b_j^T,
+// H[3p+q] = sum a_p b_q: the best rotation (b ~ R a) is the unit quaternion
+// of N's largest eigenvalue mu, and min_R sum |b - R a|^2 = S - 2 mu with
+// S = sum |a|^2 + |b|^2 -- the minimiser of the Kearsley matrix of
+// FINDROTATION (alignutils.f90:304-379), which is S I - 2 N up to the order
+// and signs of the quaternion components.  Upper-triangle entry e (row-major)
+// is +-H[i0] +- H[i1] (+- H[i2]).
+constexpr int kHornI0[10] = {0, 5, 6, 1, 0, 1, 6, 0, 5, 0};
+constexpr int kHornI1[10] = {4, 7, 2, 3, 4, 3, 2, 4, 7, 4};
+constexpr int kHornI2[10] = {8, 0, 0, 0, 8, 0, 0, 8, 0, 8};
+constexpr int kHornNeg0[10] = {0, 0, 0, 0, 0, 0, 0, 1, 0, 1};
+constexpr int kHornNeg1[10] = {0, 1, 1, 1, 1, 0, 0, 0, 0, 1};
+constexpr int kHornNeg2[10] = {0, 0, 0, 0, 1, 0, 0, 1, 0, 0};
+constexpr int kHornHas2[10] = {1, 0, 0, 0, 1, 0, 0, 1, 0, 1};
+// upper-triangle index of element (i, j) of a symmetric 4x4, row-major over (i, j)
+constexpr int kSym4[16] = {0, 1, 2, 3, 1, 4, 5, 6, 2, 5, 7, 8, 3, 6, 8, 9};
+// rotation matrix of quaternion q (row-major entry k, |q| = 1):
+// 2 (q[qa] q[qb] +- q[qc] q[qd]) - (1 on the diagonal)
+constexpr int kQuatA[9] = {0, 1, 1, 1, 0, 2, 1, 2, 0};
+constexpr int kQuatB[9] = {0, 2, 3, 2, 0, 3, 3, 3, 0};
+constexpr int kQuatC[9] = {1, 0, 0, 0, 2, 0, 0, 0, 3};
+constexpr int kQuatD[9] = {1, 3, 2, 3, 2, 1, 2, 1, 3};
+constexpr int kQuatNeg[9] = {0, 1, 0, 0, 0, 1, 1, 0, 0};
+constexpr int kQuatDiag[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+// the tables packed into integer constants for device code
+constexpr unsigned long long kHornI0p = pack_nibbles(kHornI0), kHornI1p = pack_nibbles(kHornI1),
+                             kHornI2p = pack_nibbles(kHornI2), kSym4p = pack_nibbles(kSym4),
+                             kQuatAp = pack_nibbles(kQuatA), kQuatBp = pack_nibbles(kQuatB),
+                             kQuatCp = pack_nibbles(kQuatC), kQuatDp = pack_nibbles(kQuatD);
+constexpr unsigned kHornNeg0p = pack_flags(kHornNeg0), kHornNeg1p = pack_flags(kHornNeg1),
+                   kHornNeg2p = pack_flags(kHornNeg2), kHornHas2p = pack_flags(kHornHas2),
+                   kQuatNegp = pack_flags(kQuatNeg), kQuatDiagp = pack_flags(kQuatDiag);
+
+// Euler rotation matrix (entry k, row-major) from sF = {cos a, sin a, cos b,
+// sin b, cos g, sin g, 1, 0}: +-sF[x] sF[y] sF[z] +- sF[u] sF[w], the matrix of
+// euler_matrix.
+constexpr int kEulerX[9] = {4, 5, 3, 4, 5, 3, 4, 5, 2};
+constexpr int kEulerY[9] = {2, 2, 0, 2, 2, 1, 3, 3, 6};
+constexpr int kEulerZ[9] = {0, 0, 6, 1, 1, 6, 6, 6, 6};
+constexpr int kEulerU[9] = {5, 4, 7, 5, 4, 7, 7, 7, 7};
+constexpr int kEulerW[9] = {1, 1, 7, 0, 0, 7, 7, 7, 7};
+constexpr int kEulerNeg1[9] = {0, 0, 0, 1, 1, 1, 1, 1, 0};
+constexpr int kEulerNeg2[9] = {1, 0, 0, 1, 0, 0, 0, 0, 0};
+constexpr unsigned long long kEulerXp = pack_nibbles(kEulerX), kEulerYp = pack_nibbles(kEulerY),
+                             kEulerZp = pack_nibbles(kEulerZ), kEulerUp = pack_nibbles(kEulerU),
+                             kEulerWp = pack_nibbles(kEulerW);
+constexpr unsigned kEulerNeg1p = pack_flags(kEulerNeg1), kEulerNeg2p = pack_flags(kEulerNeg2);
+
+__device__ __forceinline__ double sel3(double a0, double a1, double a2, int i) {
+    return (i == 0) ? a0 : (i == 1) ? a1 : a2;
+}
+
+// Best rotation of the moved atoms onto the fixed ones from this lane's
+// partial sums h of H (destroyed) and S.  FP32 Jacobi gives N's top
+// eigenpair (v0, mu0); one correction in the FP32 eigenbasis from the FP64
+// residual r = (N - mu0) v0, v1 = v0 + sum_k V_k (V_k . r) / (mu0 - mu_k),
+// brings v1 to FP64 accuracy, and the FP64 Rayleigh quotient of v1 gives
+// mu.  Writes R (row-major) to sR[0..8] and returns sqrt(S - 2 mu) (the
+// clamp of a negative value as in the Kearsley solution) to every lane.
+__device__ double horn_rotation(double (&h)[9], const double S, const int lane, double *sR) {
+    constexpr unsigned long long kHL9 = (unsigned long long)halve_lane(0, 9) | ((unsigned long long)halve_lane(1, 9) << 5) |
+                                        ((unsigned long long)halve_lane(2, 9) << 10) | ((unsigned long long)halve_lane(3, 9) << 15) |
+                                        ((unsigned long long)halve_lane(4, 9) << 20) | ((unsigned long long)halve_lane(5, 9) << 25) |
+                                        ((unsigned long long)halve_lane(6, 9) << 30) | ((unsigned long long)halve_lane(7, 9) << 35) |
+                                        ((unsigned long long)halve_lane(8, 9) << 40);
+    warp_halve<9>(h, lane);
+    auto hsrc = [](int k) { return (int)((kHL9 >> (5 * k)) & 31); };
+    // entry e = lane of N (lanes 10-31 repeat entry 0)
+    const int e = lane < 10 ? lane : 0;
+    const double h0 = __shfl_sync(kFull, h[0], hsrc(nibble(kHornI0p, e)));
+    const double h1 = __shfl_sync(kFull, h[0], hsrc(nibble(kHornI1p, e)));
+    const double h2 = __shfl_sync(kFull, h[0], hsrc(nibble(kHornI2p, e)));
+    const double t2 = flag(kHornHas2p, e) ? flip_sign(h2, flag(kHornNeg2p, e)) : 0.0;
+    const double ne = (flip_sign(h0, flag(kHornNeg0p, e)) + flip_sign(h1, flag(kHornNeg1p, e))) + t2;
+    // FP32 eigen-decomposition, every lane the same
+    const float nf = (float)ne;
+    float a[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i; j < 4; ++j) a[i][j] = a[j][i] = __shfl_sync(kFull, nf, nibble(kSym4p, 4 * i + j));
+    float mx = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i; j < 4; ++j) mx = fmaxf(mx, fabsf(a[i][j]));
+    if (!(mx > 0.f)) {   // H = 0: every rotation is optimal
+        if (lane < 9) sR[lane] = (lane % 4 == 0) ? 1.0 : 0.0;
+        __syncwarp();
+        return sqrt(fmax(S, 0.0));
+    }
+    const float sc = 1.f / mx;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) a[i][j] *= sc;
+    float V[4][4];
+    jacobi4f(a, V);
+    float mu[4], v0[4];
+    int jm = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        mu[k] = a[k][k] * mx;
+        if (k > 0 && mu[k] > mu[jm]) jm = k;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        v0[i] = V[i][0];
+#pragma unroll
+        for (int k = 1; k < 4; ++k)
+            if (k == jm) v0[i] = V[i][k];
+    }
+    const float mu0f = (jm == 0) ? mu[0] : (jm == 1) ? mu[1] : (jm == 2) ? mu[2] : mu[3];
+    // FP64 residual, lane i (mod 4) computes component i
+    const int i = lane & 3;
+    const double vd = (double)((i == 0) ? v0[0] : (i == 1) ? v0[1] : (i == 2) ? v0[2] : v0[3]);
+    double vj[4], nr[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        vj[j] = __shfl_sync(kFull, vd, j);
+        nr[j] = __shfl_sync(kFull, ne, nibble(kSym4p, 4 * i + j));
+    }
+    double r = nr[0] * vj[0];
+    r = fma(nr[1], vj[1], r);
+    r = fma(nr[2], vj[2], r);
+    r = fma(nr[3], vj[3], r);
+    r = fma(flip_sign((double)mu0f, true), vd, r);
+    const float rf = (float)r;
+    float rr[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) rr[j] = __shfl_sync(kFull, rf, j);
+    // correction in the FP32 eigenbasis (components with no gap are left out)
+    float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float gap = mu0f - mu[k];
+        if (k == jm || !(gap > 1e-6f * mx)) continue;
+        const float cf = (V[0][k] * rr[0] + V[1][k] * rr[1] + V[2][k] * rr[2] + V[3][k] * rr[3]) / gap;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d[j] = fmaf(cf, V[j][k], d[j]);
+    }
+    if (!(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3] < 1e-6f))   // no contraction
+        d[0] = d[1] = d[2] = d[3] = 0.f;
+    const double v1 = vd + (double)((i == 0) ? d[0] : (i == 1) ? d[1] : (i == 2) ? d[2] : d[3]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) vj[j] = __shfl_sync(kFull, v1, j);
+    double nv = nr[0] * vj[0];
+    nv = fma(nr[1], vj[1], nv);
+    nv = fma(nr[2], vj[2], nv);
+    nv = fma(nr[3], vj[3], nv);
+    // v1.N v1 on even lanes, |v1|^2 on odd lanes of each group of 4
+    const bool odd = lane & 1;
+    const double t = v1 * nv, w = v1 * v1;
+    double x = (odd ? w : t) + __shfl_xor_sync(kFull, odd ? t : w, 1);
+    x += __shfl_xor_sync(kFull, x, 2);
+    const double num = __shfl_sync(kFull, x, 0), den = __shfl_sync(kFull, x, 1);
+    const double inv = 1.0 / den;
+    double lam = fma(-2.0, num * inv, S);
+    if (lam < 0.0) lam = (fabs(lam) < 1e-6) ? 0.0 : -lam;
+    // rotation matrix, entry k on lane k
+    const int k = lane < 9 ? lane : 0;
+    auto q = [&](int c) { return (c == 0) ? vj[0] : (c == 1) ? vj[1] : (c == 2) ? vj[2] : vj[3]; };
+    double p = q(nibble(kQuatAp, k)) * q(nibble(kQuatBp, k));
+    p = fma(flip_sign(q(nibble(kQuatCp, k)), flag(kQuatNegp, k)),
+            q(nibble(kQuatDp, k)), p);
+    const double Rk = fma(inv + inv, p, flag(kQuatDiagp, k) ? -1.0 : 0.0);
+    if (lane < 9) sR[lane] = Rk;
+    __syncwarp();
+    return sqrt(lam);
+}
+
+// sRb <- sRn sRb (lanes 0-8); then the affine map of the input coordinates
+// that gives the moved structure, x -> T x + t with T = sRb sRs and
+// t = add - sRb ca, into sT[0..8] (T, row-major) and sT[9..11] (t).
+__device__ __forceinline__ void compose_affine(const double *sRn, double *sRb, const double *sRs, const double (&nca)[3],
+                                               const double (&add)[3], double *sT, const int lane) {
+    const int k = lane < 9 ? lane : 0, r = k / 3, c = k % 3;
+    double v = sRn[3 * r] * sRb[c];
+    v = fma(sRn[3 * r + 1], sRb[3 + c], v);
+    v = fma(sRn[3 * r + 2], sRb[6 + c], v);
+    __syncwarp();
+    if (lane < 9) sRb[lane] = v;
+    __syncwarp();
+    const bool tl = lane >= 9;   // lanes 9-11: translation
+    const int rr = tl ? ((lane < 12) ? lane - 9 : 0) : r;
+    const double x0 = tl ? nca[0] : sRs[c], x1 = tl ? nca[1] : sRs[3 + c], x2 = tl ? nca[2] : sRs[6 + c];
+    double w = fma(sRb[3 * rr], x0, tl ? sel3(add[0], add[1], add[2], rr) : 0.0);
+    w = fma(sRb[3 * rr + 1], x1, w);
+    w = fma(sRb[3 * rr + 2], x2, w);
+    if (lane < 12) sT[lane] = w;
+    __syncwarp();
+}
+
 // The m nearest columns of one row as the binary max-heap of PAIRDISTS
 // (alignutils.f90:641-701): the first m columns are sifted up in order, each
 // later closer column replaces the root and is sifted down.  The heap's array
@@ -707,7 +1005,6 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     constexpr bool kF32 = sizeof(DT) == 4;
     static_assert(kF32 || !RECOMP, "costs are recomputed only from FP32 coordinates");
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double sRb[9], sRn[9], sRc[9];
     const int lane = threadIdx.x;
     const int c = cand_list[blockIdx.x];
     const int p = cand2pair[c];
@@ -731,111 +1028,455 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     const long long ob = P.candatom0 + (long long)local * n;
     double *DA = cxyz + 3 * ob;                            // moved structure, FP64
     const double *XA = xa + 3LL * a0, *XB = xb + 3LL * a0;   // inputs of the pair
-    double d0[3] = {0, 0, 0};
-    if (lane == 0) {
-        for (int k = 0; k < 9; ++k) { sRb[k] = (k % 4 == 0) ? 1.0 : 0.0; sRc[k] = sRb[k]; }
-        if (!bulk) {
-            const double conv = FO_PI / P.G;
-            euler_matrix((pk[0] - 1.0) * 2 * conv, (pk[1] - 0.5) * conv, (pk[2] - 1.0) * 2 * conv, sRc);
-        }
-    }
-    if (bulk)
-        for (int k = 0; k < 3; ++k) d0[k] = (pk[k] - 1.0) * box[k] / P.G;
-    __syncwarp();
-    const double sgn = (o == 1) ? -1.0 : 1.0;
-    // moved atom j rotated by the candidate (cluster) or shifted (bulk)
-    auto a_raw = [&](int j, double *out) {
-        const double *a = XA + 3 * j;
-        if (bulk) {
-            for (int k = 0; k < 3; ++k) out[k] = a[k] - d0[k];
+    if constexpr (kF32 && RECOMP) {
+        // Mixed form: FP32 coordinates for the costs, FP64 superposition built
+        // from few FP64 instructions (Horn rotation, one affine map per step).
+        __shared__ double sRb[9], sRn[9], sRc[9], sRs[9], sT[12], sF[8];
+        GroupCoords GC;
+        GC.bulk = bulk;
+        GC.xb = XB;
+        double S = 0, d0[3] = {0, 0, 0}, rb[3] = {0, 0, 0}, nbox[3], off[3] = {0, 0, 0}, nca[3] = {0, 0, 0};
+        const double zero3[3] = {0, 0, 0};
+        for (int k = 0; k < 3; ++k) nbox[k] = flip_sign(box[k], true);
+        if constexpr (BOX) {
+            // lanes 0-2: shift of the candidate (peak_k - 1) box_k / G; lanes 3-5: 1 / box_k
+            const int k = lane % 3;
+            const double bk = sel3(box[0], box[1], box[2], k);
+            const double num = (lane < 3) ? (pk[k] - 1.0) * bk : 1.0;
+            const double den = (lane < 3) ? (double)P.G : bk;
+            const double qv = (den != 0.0) ? num / den : 0.0;
+            for (int j = 0; j < 3; ++j) {
+                d0[j] = __shfl_sync(kFull, qv, j);
+                rb[j] = __shfl_sync(kFull, qv, 3 + j);
+                off[j] = flip_sign(d0[j], true);
+                GC.cmb[j] = 0.0;
+                GC.box[j] = box[j];
+                GC.bxf[j] = (float)box[j];
+                GC.rxf[j] = (float)rb[j];
+            }
+            for (int j = lane; j < n; j += 32) {
+                double a[3];
+                for (int r = 0; r < 3; ++r) {
+                    a[r] = XA[3 * j + r] + off[r];
+                    DA[3 * j + r] = a[r];
+                }
+                A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
+                B4[j] = make_float4((float)XB[3 * j], (float)XB[3 * j + 1], (float)XB[3 * j + 2], 0.f);
+                permbest[j] = j;
+            }
         } else {
-            for (int k = 0; k < 3; ++k)
-                out[k] = sgn * (sRc[3 * k] * a[0] + sRc[3 * k + 1] * a[1] + sRc[3 * k + 2] * a[2]);
-        }
-    };
-    double cs[6] = {0, 0, 0, 0, 0, 0};
-    for (int j = lane; j < n; j += 32) {
-        double t[3];
-        a_raw(j, t);
-        for (int k = 0; k < 3; ++k) { cs[k] += t[k]; cs[3 + k] += XB[3 * j + k]; }
-    }
-    for (int k = 0; k < 6; ++k) cs[k] = wsum_d(cs[k]);
-    // ITERATIVEALIGN works on structures centred at their centroids
-    double ca[3] = {0, 0, 0};
-    GroupCoords GC;
-    GC.bulk = bulk;
-    for (int k = 0; k < 3; ++k) {
-        GC.cmb[k] = bulk ? 0.0 : cs[3 + k] / n;
-        ca[k] = cs[k] / n;
-        GC.box[k] = box[k];
-        GC.bxf[k] = (float)box[k];
-        GC.rxf[k] = box[k] != 0.0 ? (float)(1.0 / box[k]) : 0.f;
-    }
-    // starting moved structure A0 (centred for clusters)
-    auto a_start = [&](int j, double *out) {
-        a_raw(j, out);
-        if (!bulk)
-            for (int k = 0; k < 3; ++k) out[k] -= ca[k];
-    };
-    GC.xb = XB;
-    for (int j = lane; j < n; j += 32) {
-        double a[3];
-        a_start(j, a);
-        for (int k = 0; k < 3; ++k) DA[3 * j + k] = a[k];
-        if constexpr (kF32) {
-            double b[3];
-            GC.b(j, b);
-            A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
-            B4[j] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.f);
-        }
-        permbest[j] = j;
-    }
-    __syncwarp();
-    const GroupCoords GB = GC;   // whole-structure view of the fixed structure
-    double db[3] = {0, 0, 0}, newdist = 0;
-    int ntries = 0, nperm = n, fail = 0;
-    for (int iter = 0; iter < 64 && nperm > 0; ++iter) {
-        for (int j = lane; j < n; j += 32) newperm[j] = j;
-        double pdsum = 0;
-        __syncwarp();
-        for (int gi = 0; gi < P.ngroups; ++gi) {
-            const GroupDev g = groups[P.group0 + gi];
-            const int ns = g.n, m = g.m, s0 = g.slot0 - a0;
-            GC.xb = XB + 3 * s0;
-            GC.A = DA + 3 * s0;
-            GC.B4 = B4 + s0;
-            GC.A4 = A4 + s0;
-            const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L)
-                                            : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L);
-            if (rc) fail += 1;
+            // Euler angles of the candidate over pi: lanes 0-2 take sin and cos of one each
+            const double num = (lane == 1) ? pk[1] - 0.5 : (pk[(lane < 3) ? lane : 0] - 1.0) * 2.0;
+            double sn, cs;
+            sincospi(num / (double)P.G, &sn, &cs);
+            if (lane < 3) { sF[2 * lane] = cs; sF[2 * lane + 1] = sn; }
+            if (lane == 3) { sF[6] = 1.0; sF[7] = 0.0; }
             __syncwarp();
-            for (int i = lane; i < ns; i += 32) {
-                int col = lx[i];
-                if (col >= ns) { col = ns - 1; fail += 1; }
-                if (col < 0) { col = 0; fail += 1; }
-                newperm[s0 + i] = s0 + col;
-                double b[3];
-                GC.b(i, b);
-                pdsum += pdist2<double>(b, DA + 3 * (s0 + col), bulk, box);
+            const int k = lane < 9 ? lane : 0;
+            double rc = sF[nibble(kEulerXp, k)] * sF[nibble(kEulerYp, k)];
+            rc = rc * sF[nibble(kEulerZp, k)];
+            rc = fma(flip_sign(sF[nibble(kEulerUp, k)], flag(kEulerNeg2p, k)), sF[nibble(kEulerWp, k)],
+                     flip_sign(rc, flag(kEulerNeg1p, k)));
+            if (lane < 9) {
+                sRc[lane] = rc;
+                sRs[lane] = flip_sign(rc, o == 1);   // with the inversion
+                sRb[lane] = (lane % 4 == 0) ? 1.0 : 0.0;
+            }
+            // centroids of both inputs
+            double v6[6] = {0, 0, 0, 0, 0, 0};
+            for (int j = lane; j < n; j += 32)
+                for (int r = 0; r < 3; ++r) {
+                    v6[r] += XA[3 * j + r];
+                    v6[3 + r] += XB[3 * j + r];
+                }
+            warp_halve<6>(v6, lane);
+            const double mean = v6[0] / n;
+            double mx[6];
+            for (int r = 0; r < 6; ++r) mx[r] = __shfl_sync(kFull, mean, halve_lane(r, 6));
+            __syncwarp();
+            // centroid of the rotated moved structure, lanes 0-2
+            const int r3 = lane % 3;
+            double cv = sRs[3 * r3] * mx[0];
+            cv = fma(sRs[3 * r3 + 1], mx[1], cv);
+            cv = fma(sRs[3 * r3 + 2], mx[2], cv);
+            for (int r = 0; r < 3; ++r) {
+                nca[r] = flip_sign(__shfl_sync(kFull, cv, r), true);
+                GC.cmb[r] = mx[3 + r];
+                GC.box[r] = box[r];
+                GC.bxf[r] = 0.f;
+                GC.rxf[r] = 0.f;
+            }
+            double Rs[9];
+            for (int r = 0; r < 9; ++r) Rs[r] = sRs[r];
+            double s = 0;
+            for (int j = lane; j < n; j += 32) {
+                const double x0 = XA[3 * j], x1 = XA[3 * j + 1], x2 = XA[3 * j + 2];
+                double a[3], b[3];
+                GC.b(j, b);
+                for (int r = 0; r < 3; ++r) {
+                    a[r] = fma(Rs[3 * r], x0, fma(Rs[3 * r + 1], x1, fma(Rs[3 * r + 2], x2, nca[r])));
+                    DA[3 * j + r] = a[r];
+                    s = fma(a[r], a[r], s);
+                    s = fma(b[r], b[r], s);
+                }
+                A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
+                B4[j] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.f);
+                permbest[j] = j;
+            }
+            S = wsum_d(s);
+        }
+        __syncwarp();
+        const GroupCoords GB = GC;   // whole-structure view of the fixed structure
+        const double thr = sqrt((double)n) / kPScale;
+        double db[3] = {0, 0, 0}, newdist = 0;
+        int ntries = 0, nperm = n, fail = 0;
+        // mean minimum-image displacement of the moved atoms (a(j)) onto the
+        // fixed ones, and the distance after that shift
+        auto displacement = [&](const auto &a_of, double *dn) {
+            double v3[3] = {0, 0, 0};
+            for (int j = lane; j < n; j += 32) {
+                const double *a = a_of(j);
+                for (int r = 0; r < 3; ++r) {
+                    const double t = XB[3 * j + r] - a[r];
+                    v3[r] += fma(nbox[r], rint(t * rb[r]), t);
+                }
+            }
+            warp_halve<3>(v3, lane);
+            const double mv = v3[0] / n;
+            for (int r = 0; r < 3; ++r) dn[r] = __shfl_sync(kFull, mv, halve_lane(r, 3));
+            double s1 = 0;
+            for (int j = lane; j < n; j += 32) {
+                const double *a = a_of(j);
+                for (int r = 0; r < 3; ++r) {
+                    double t = (XB[3 * j + r] - a[r]) - dn[r];
+                    t = fma(nbox[r], rint(t * rb[r]), t);
+                    s1 = fma(t, t, s1);
+                }
+            }
+            return sqrt(wsum_d(s1));
+        };
+        for (int iter = 0; iter < 64 && nperm > 0; ++iter) {
+            for (int j = lane; j < n; j += 32) newperm[j] = j;
+            double pdsum = 0;
+            __syncwarp();
+            for (int gi = 0; gi < P.ngroups; ++gi) {
+                const GroupDev g = groups[P.group0 + gi];
+                const int ns = g.n, m = g.m, s0 = g.slot0 - a0;
+                GC.xb = XB + 3 * s0;
+                GC.A = DA + 3 * s0;
+                GC.B4 = B4 + s0;
+                GC.A4 = A4 + s0;
+                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L)
+                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L);
+                if (rc) fail += 1;
+                __syncwarp();
+                for (int i = lane; i < ns; i += 32) {
+                    int col = lx[i];
+                    if (col >= ns) { col = ns - 1; fail += 1; }
+                    if (col < 0) { col = 0; fail += 1; }
+                    newperm[s0 + i] = s0 + col;
+                    const double *a = DA + 3 * (s0 + col);
+                    if constexpr (BOX) {
+                        for (int r = 0; r < 3; ++r) {
+                            double t = GC.xb[3 * i + r] - a[r];
+                            t = fma(nbox[r], rint(t * rb[r]), t);
+                            pdsum = fma(t, t, pdsum);
+                        }
+                    } else {
+                        double b[3];
+                        GC.b(i, b);
+                        pdsum += pdist2<double>(b, a, 0, box);
+                    }
+                }
+                __syncwarp();
+            }
+            pdsum = wsum_d(pdsum);
+            int cnt = 0;
+            for (int j = lane; j < n; j += 32) {
+                int q = newperm[j];
+                ptmp[j] = permbest[q];
+                if (q != j) ++cnt;
+            }
+            for (int o2 = 16; o2 > 0; o2 >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o2);
+            if constexpr (BOX) {
+                double dn[3];
+                newdist = displacement([&](int j) { return DA + 3 * newperm[j]; }, dn);
+                for (int r = 0; r < 3; ++r) {
+                    db[r] += dn[r];
+                    off[r] += dn[r];
+                }
+                __syncwarp();
+                for (int j = lane; j < n; j += 32) {
+                    const int pj = ptmp[j];
+                    permbest[j] = pj;
+                    double a[3];
+                    for (int r = 0; r < 3; ++r) {
+                        a[r] = XA[3 * pj + r] + off[r];
+                        DA[3 * j + r] = a[r];
+                    }
+                    A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
+                }
+            } else {
+                double h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                for (int j = lane; j < n; j += 32) {
+                    const double *a = DA + 3 * newperm[j];
+                    const double a3[3] = {a[0], a[1], a[2]};
+                    double b[3];
+                    GB.b(j, b);
+                    for (int p2 = 0; p2 < 3; ++p2)
+                        for (int q2 = 0; q2 < 3; ++q2) h[3 * p2 + q2] = fma(a3[p2], b[q2], h[3 * p2 + q2]);
+                }
+                newdist = horn_rotation(h, S, lane, sRn);
+                compose_affine(sRn, sRb, sRs, nca, zero3, sT, lane);
+                double T[12];
+                for (int r = 0; r < 12; ++r) T[r] = sT[r];
+                for (int j = lane; j < n; j += 32) {
+                    const int pj = ptmp[j];
+                    permbest[j] = pj;
+                    const double x0 = XA[3 * pj], x1 = XA[3 * pj + 1], x2 = XA[3 * pj + 2];
+                    double a[3];
+                    for (int r = 0; r < 3; ++r) {
+                        a[r] = fma(T[3 * r], x0, fma(T[3 * r + 1], x1, fma(T[3 * r + 2], x2, T[9 + r])));
+                        DA[3 * j + r] = a[r];
+                    }
+                    A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
+                }
             }
             __syncwarp();
+            nperm = cnt;
+            ntries += 1;
+            // (newdist - pd) / newdist > sqrt(n) / PSCALE, without the division
+            const double pd = sqrt(pdsum);
+            if (newdist - pd > thr * newdist) nperm = 0;
+            if (ntries > kMaxTries) nperm = 0;
         }
-        pdsum = wsum_d(pdsum);
-        int cnt = 0;
+        // final superposition without a new permutation
+        if constexpr (BOX) {
+            double dn[3];
+            newdist = displacement([&](int j) { return DA + 3 * j; }, dn);
+            for (int r = 0; r < 3; ++r) db[r] += dn[r];
+            __syncwarp();
+            for (int j = lane; j < n; j += 32)
+                for (int r = 0; r < 3; ++r) DA[3 * j + r] += dn[r];
+        } else {
+            double h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (int j = lane; j < n; j += 32) {
+                const double a3[3] = {DA[3 * j], DA[3 * j + 1], DA[3 * j + 2]};
+                double b[3];
+                GB.b(j, b);
+                for (int p2 = 0; p2 < 3; ++p2)
+                    for (int q2 = 0; q2 < 3; ++q2) h[3 * p2 + q2] = fma(a3[p2], b[q2], h[3 * p2 + q2]);
+            }
+            newdist = horn_rotation(h, S, lane, sRn);
+            compose_affine(sRn, sRb, sRs, nca, GB.cmb, sT, lane);   // back to the fixed centroid
+            double T[12];
+            for (int r = 0; r < 12; ++r) T[r] = sT[r];
+            for (int j = lane; j < n; j += 32) {
+                const int pj = permbest[j];
+                const double x0 = XA[3 * pj], x1 = XA[3 * pj + 1], x2 = XA[3 * pj + 2];
+                for (int r = 0; r < 3; ++r)
+                    DA[3 * j + r] = fma(T[3 * r], x0, fma(T[3 * r + 1], x1, fma(T[3 * r + 2], x2, T[9 + r])));
+            }
+        }
+        __syncwarp();
+        for (int j = lane; j < n; j += 32) cperm[ob + j] = permbest[j];
+        for (int o2 = 16; o2 > 0; o2 >>= 1) fail += __shfl_xor_sync(kFull, fail, o2);
+        if constexpr (BOX) {
+            if (lane < 9) cR[9LL * c + lane] = (lane % 4 == 0) ? 1.0 : 0.0;
+        } else {   // rotation of the input: sRb sRc, entry k on lane k
+            const int k = lane < 9 ? lane : 0, r = k / 3, cc = k % 3;
+            double v = sRb[3 * r] * sRc[cc];
+            v = fma(sRb[3 * r + 1], sRc[3 + cc], v);
+            v = fma(sRb[3 * r + 2], sRc[6 + cc], v);
+            if (lane < 9) cR[9LL * c + lane] = v;
+        }
+        if (lane == 0) {
+            cdist[c] = newdist;
+            for (int k = 0; k < 3; ++k) cdisp[3LL * c + k] = db[k] - d0[k];
+            cniter[c] = ntries;
+            cstat[c] = fail ? (int)ST_LAP_FAILED : 0;
+        }
+    } else {
+        __shared__ double sRb[9], sRn[9], sRc[9];
+        double d0[3] = {0, 0, 0};
+        if (lane == 0) {
+            for (int k = 0; k < 9; ++k) { sRb[k] = (k % 4 == 0) ? 1.0 : 0.0; sRc[k] = sRb[k]; }
+            if (!bulk) {
+                const double conv = FO_PI / P.G;
+                euler_matrix((pk[0] - 1.0) * 2 * conv, (pk[1] - 0.5) * conv, (pk[2] - 1.0) * 2 * conv, sRc);
+            }
+        }
+        if (bulk)
+            for (int k = 0; k < 3; ++k) d0[k] = (pk[k] - 1.0) * box[k] / P.G;
+        __syncwarp();
+        const double sgn = (o == 1) ? -1.0 : 1.0;
+        // moved atom j rotated by the candidate (cluster) or shifted (bulk)
+        auto a_raw = [&](int j, double *out) {
+            const double *a = XA + 3 * j;
+            if (bulk) {
+                for (int k = 0; k < 3; ++k) out[k] = a[k] - d0[k];
+            } else {
+                for (int k = 0; k < 3; ++k)
+                    out[k] = sgn * (sRc[3 * k] * a[0] + sRc[3 * k + 1] * a[1] + sRc[3 * k + 2] * a[2]);
+            }
+        };
+        double cs[6] = {0, 0, 0, 0, 0, 0};
         for (int j = lane; j < n; j += 32) {
-            int q = newperm[j];
-            ptmp[j] = permbest[q];
-            if (q != j) ++cnt;
+            double t[3];
+            a_raw(j, t);
+            for (int k = 0; k < 3; ++k) { cs[k] += t[k]; cs[3 + k] += XB[3 * j + k]; }
         }
-        for (int o2 = 16; o2 > 0; o2 >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o2);
+        for (int k = 0; k < 6; ++k) cs[k] = wsum_d(cs[k]);
+        // ITERATIVEALIGN works on structures centred at their centroids
+        double ca[3] = {0, 0, 0};
+        GroupCoords GC;
+        GC.bulk = bulk;
+        for (int k = 0; k < 3; ++k) {
+            GC.cmb[k] = bulk ? 0.0 : cs[3 + k] / n;
+            ca[k] = cs[k] / n;
+            GC.box[k] = box[k];
+            GC.bxf[k] = (float)box[k];
+            GC.rxf[k] = box[k] != 0.0 ? (float)(1.0 / box[k]) : 0.f;
+        }
+        // starting moved structure A0 (centred for clusters)
+        auto a_start = [&](int j, double *out) {
+            a_raw(j, out);
+            if (!bulk)
+                for (int k = 0; k < 3; ++k) out[k] -= ca[k];
+        };
+        GC.xb = XB;
+        for (int j = lane; j < n; j += 32) {
+            double a[3];
+            a_start(j, a);
+            for (int k = 0; k < 3; ++k) DA[3 * j + k] = a[k];
+            if constexpr (kF32) {
+                double b[3];
+                GC.b(j, b);
+                A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
+                B4[j] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.f);
+            }
+            permbest[j] = j;
+        }
+        __syncwarp();
+        const GroupCoords GB = GC;   // whole-structure view of the fixed structure
+        double db[3] = {0, 0, 0}, newdist = 0;
+        int ntries = 0, nperm = n, fail = 0;
+        for (int iter = 0; iter < 64 && nperm > 0; ++iter) {
+            for (int j = lane; j < n; j += 32) newperm[j] = j;
+            double pdsum = 0;
+            __syncwarp();
+            for (int gi = 0; gi < P.ngroups; ++gi) {
+                const GroupDev g = groups[P.group0 + gi];
+                const int ns = g.n, m = g.m, s0 = g.slot0 - a0;
+                GC.xb = XB + 3 * s0;
+                GC.A = DA + 3 * s0;
+                GC.B4 = B4 + s0;
+                GC.A4 = A4 + s0;
+                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L)
+                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L);
+                if (rc) fail += 1;
+                __syncwarp();
+                for (int i = lane; i < ns; i += 32) {
+                    int col = lx[i];
+                    if (col >= ns) { col = ns - 1; fail += 1; }
+                    if (col < 0) { col = 0; fail += 1; }
+                    newperm[s0 + i] = s0 + col;
+                    double b[3];
+                    GC.b(i, b);
+                    pdsum += pdist2<double>(b, DA + 3 * (s0 + col), bulk, box);
+                }
+                __syncwarp();
+            }
+            pdsum = wsum_d(pdsum);
+            int cnt = 0;
+            for (int j = lane; j < n; j += 32) {
+                int q = newperm[j];
+                ptmp[j] = permbest[q];
+                if (q != j) ++cnt;
+            }
+            for (int o2 = 16; o2 > 0; o2 >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o2);
+            if (bulk) {
+                double s3[3] = {0, 0, 0};
+                for (int j = lane; j < n; j += 32) {
+                    const double *a = DA + 3 * newperm[j];
+                    double b[3];
+                    GB.b(j, b);
+                    for (int k = 0; k < 3; ++k) {
+                        double t = b[k] - a[k];
+                        s3[k] += t - box[k] * round(t / box[k]);
+                    }
+                }
+                double dn[3];
+                for (int k = 0; k < 3; ++k) dn[k] = wsum_d(s3[k]) / n;
+                double s1 = 0;
+                for (int j = lane; j < n; j += 32) {
+                    const double *a = DA + 3 * newperm[j];
+                    double ad[3] = {a[0] + dn[0], a[1] + dn[1], a[2] + dn[2]}, b[3];
+                    GB.b(j, b);
+                    s1 += pdist2<double>(b, ad, 1, box);
+                }
+                newdist = sqrt(wsum_d(s1));
+                for (int k = 0; k < 3; ++k) db[k] += dn[k];
+                __syncwarp();
+                for (int j = lane; j < n; j += 32) {
+                    permbest[j] = ptmp[j];
+                    double a[3];
+                    a_start(ptmp[j], a);
+                    for (int k = 0; k < 3; ++k) DA[3 * j + k] = a[k] + db[k];
+                    if constexpr (kF32)
+                        A4[j] = make_float4((float)DA[3 * j], (float)DA[3 * j + 1], (float)DA[3 * j + 2], 0.f);
+                }
+            } else {
+                double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+                for (int j = lane; j < n; j += 32) {
+                    const double *a = DA + 3 * newperm[j];
+                    double b[3];
+                    GB.b(j, b);
+                    double xm = b[0] - a[0], ym = b[1] - a[1], zm = b[2] - a[2];
+                    double xp = b[0] + a[0], yp = b[1] + a[1], zp = b[2] + a[2];
+                    q[0] += xm * xm + ym * ym + zm * zm;
+                    q[1] += yp * zm - ym * zp;
+                    q[2] += xm * zp - xp * zm;
+                    q[3] += xp * ym - xm * yp;
+                    q[4] += yp * yp + zp * zp + xm * xm;
+                    q[5] += xm * ym - xp * yp;
+                    q[6] += xm * zm - xp * zp;
+                    q[7] += xp * xp + zp * zp + ym * ym;
+                    q[8] += ym * zm - yp * zp;
+                    q[9] += xp * xp + yp * yp + zm * zm;
+                }
+                for (int k = 0; k < 10; ++k) q[k] = wsum_d(q[k]);
+                if (lane == 0) {
+                    newdist = kearsley_rotation_fast(q, sRn);
+                    matmul3(sRn, sRb, sRb);
+                }
+                newdist = __shfl_sync(kFull, newdist, 0);
+                __syncwarp();
+                for (int j = lane; j < n; j += 32) {
+                    permbest[j] = ptmp[j];
+                    double a[3];
+                    a_start(ptmp[j], a);
+                    for (int k = 0; k < 3; ++k)
+                        DA[3 * j + k] = sRb[3 * k] * a[0] + sRb[3 * k + 1] * a[1] + sRb[3 * k + 2] * a[2];
+                    if constexpr (kF32)
+                        A4[j] = make_float4((float)DA[3 * j], (float)DA[3 * j + 1], (float)DA[3 * j + 2], 0.f);
+                }
+            }
+            __syncwarp();
+            nperm = cnt;
+            ntries += 1;
+            double pd = sqrt(pdsum);
+            if ((newdist - pd) / newdist > sqrt((double)n) / kPScale) nperm = 0;
+            if (ntries > kMaxTries) nperm = 0;
+        }
+        // final minimisation without a new permutation
         if (bulk) {
             double s3[3] = {0, 0, 0};
             for (int j = lane; j < n; j += 32) {
-                const double *a = DA + 3 * newperm[j];
                 double b[3];
                 GB.b(j, b);
                 for (int k = 0; k < 3; ++k) {
-                    double t = b[k] - a[k];
+                    double t = b[k] - DA[3 * j + k];
                     s3[k] += t - box[k] * round(t / box[k]);
                 }
             }
@@ -843,26 +1484,19 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
             for (int k = 0; k < 3; ++k) dn[k] = wsum_d(s3[k]) / n;
             double s1 = 0;
             for (int j = lane; j < n; j += 32) {
-                const double *a = DA + 3 * newperm[j];
-                double ad[3] = {a[0] + dn[0], a[1] + dn[1], a[2] + dn[2]}, b[3];
+                double ad[3] = {DA[3 * j] + dn[0], DA[3 * j + 1] + dn[1], DA[3 * j + 2] + dn[2]}, b[3];
                 GB.b(j, b);
                 s1 += pdist2<double>(b, ad, 1, box);
             }
             newdist = sqrt(wsum_d(s1));
             for (int k = 0; k < 3; ++k) db[k] += dn[k];
             __syncwarp();
-            for (int j = lane; j < n; j += 32) {
-                permbest[j] = ptmp[j];
-                double a[3];
-                a_start(ptmp[j], a);
-                for (int k = 0; k < 3; ++k) DA[3 * j + k] = a[k] + db[k];
-                if constexpr (kF32)
-                    A4[j] = make_float4((float)DA[3 * j], (float)DA[3 * j + 1], (float)DA[3 * j + 2], 0.f);
-            }
+            for (int j = lane; j < n; j += 32)
+                for (int k = 0; k < 3; ++k) DA[3 * j + k] += dn[k];
         } else {
             double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
             for (int j = lane; j < n; j += 32) {
-                const double *a = DA + 3 * newperm[j];
+                const double *a = DA + 3 * j;
                 double b[3];
                 GB.b(j, b);
                 double xm = b[0] - a[0], ym = b[1] - a[1], zm = b[2] - a[2];
@@ -886,89 +1520,23 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
             newdist = __shfl_sync(kFull, newdist, 0);
             __syncwarp();
             for (int j = lane; j < n; j += 32) {
-                permbest[j] = ptmp[j];
-                double a[3];
-                a_start(ptmp[j], a);
+                double a[3] = {DA[3 * j], DA[3 * j + 1], DA[3 * j + 2]};
                 for (int k = 0; k < 3; ++k)
-                    DA[3 * j + k] = sRb[3 * k] * a[0] + sRb[3 * k + 1] * a[1] + sRb[3 * k + 2] * a[2];
-                if constexpr (kF32)
-                    A4[j] = make_float4((float)DA[3 * j], (float)DA[3 * j + 1], (float)DA[3 * j + 2], 0.f);
+                    DA[3 * j + k] = sRn[3 * k] * a[0] + sRn[3 * k + 1] * a[1] + sRn[3 * k + 2] * a[2] + GB.cmb[k];
             }
         }
         __syncwarp();
-        nperm = cnt;
-        ntries += 1;
-        double pd = sqrt(pdsum);
-        if ((newdist - pd) / newdist > sqrt((double)n) / kPScale) nperm = 0;
-        if (ntries > kMaxTries) nperm = 0;
-    }
-    // final minimisation without a new permutation
-    if (bulk) {
-        double s3[3] = {0, 0, 0};
-        for (int j = lane; j < n; j += 32) {
-            double b[3];
-            GB.b(j, b);
-            for (int k = 0; k < 3; ++k) {
-                double t = b[k] - DA[3 * j + k];
-                s3[k] += t - box[k] * round(t / box[k]);
-            }
-        }
-        double dn[3];
-        for (int k = 0; k < 3; ++k) dn[k] = wsum_d(s3[k]) / n;
-        double s1 = 0;
-        for (int j = lane; j < n; j += 32) {
-            double ad[3] = {DA[3 * j] + dn[0], DA[3 * j + 1] + dn[1], DA[3 * j + 2] + dn[2]}, b[3];
-            GB.b(j, b);
-            s1 += pdist2<double>(b, ad, 1, box);
-        }
-        newdist = sqrt(wsum_d(s1));
-        for (int k = 0; k < 3; ++k) db[k] += dn[k];
-        __syncwarp();
-        for (int j = lane; j < n; j += 32)
-            for (int k = 0; k < 3; ++k) DA[3 * j + k] += dn[k];
-    } else {
-        double q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int j = lane; j < n; j += 32) {
-            const double *a = DA + 3 * j;
-            double b[3];
-            GB.b(j, b);
-            double xm = b[0] - a[0], ym = b[1] - a[1], zm = b[2] - a[2];
-            double xp = b[0] + a[0], yp = b[1] + a[1], zp = b[2] + a[2];
-            q[0] += xm * xm + ym * ym + zm * zm;
-            q[1] += yp * zm - ym * zp;
-            q[2] += xm * zp - xp * zm;
-            q[3] += xp * ym - xm * yp;
-            q[4] += yp * yp + zp * zp + xm * xm;
-            q[5] += xm * ym - xp * yp;
-            q[6] += xm * zm - xp * zp;
-            q[7] += xp * xp + zp * zp + ym * ym;
-            q[8] += ym * zm - yp * zp;
-            q[9] += xp * xp + yp * yp + zm * zm;
-        }
-        for (int k = 0; k < 10; ++k) q[k] = wsum_d(q[k]);
+        for (int j = lane; j < n; j += 32) cperm[ob + j] = permbest[j];
+        for (int o2 = 16; o2 > 0; o2 >>= 1) fail += __shfl_xor_sync(kFull, fail, o2);
         if (lane == 0) {
-            newdist = kearsley_rotation_fast(q, sRn);
-            matmul3(sRn, sRb, sRb);
+            cdist[c] = newdist;
+            double R[9];
+            matmul3(sRb, sRc, R);
+            for (int k = 0; k < 9; ++k) cR[9LL * c + k] = bulk ? ((k % 4 == 0) ? 1.0 : 0.0) : R[k];
+            for (int k = 0; k < 3; ++k) cdisp[3LL * c + k] = db[k] - d0[k];
+            cniter[c] = ntries;
+            cstat[c] = fail ? (int)ST_LAP_FAILED : 0;
         }
-        newdist = __shfl_sync(kFull, newdist, 0);
-        __syncwarp();
-        for (int j = lane; j < n; j += 32) {
-            double a[3] = {DA[3 * j], DA[3 * j + 1], DA[3 * j + 2]};
-            for (int k = 0; k < 3; ++k)
-                DA[3 * j + k] = sRn[3 * k] * a[0] + sRn[3 * k + 1] * a[1] + sRn[3 * k + 2] * a[2] + GB.cmb[k];
-        }
-    }
-    __syncwarp();
-    for (int j = lane; j < n; j += 32) cperm[ob + j] = permbest[j];
-    for (int o2 = 16; o2 > 0; o2 >>= 1) fail += __shfl_xor_sync(kFull, fail, o2);
-    if (lane == 0) {
-        cdist[c] = newdist;
-        double R[9];
-        matmul3(sRb, sRc, R);
-        for (int k = 0; k < 9; ++k) cR[9LL * c + k] = bulk ? ((k % 4 == 0) ? 1.0 : 0.0) : R[k];
-        for (int k = 0; k < 3; ++k) cdisp[3LL * c + k] = db[k] - d0[k];
-        cniter[c] = ntries;
-        cstat[c] = fail ? (int)ST_LAP_FAILED : 0;
     }
 }
 
