@@ -457,10 +457,10 @@ def main():
     achieved = byts / (top_ms / 1000.0) / 1e9
     # DRAM bytes (read + write) the kernel moves, from an ncu capture of a
     # 256-pair case of this workload, scaled by the units of the step:
-    # refinement 2.4 KB per candidate (its data stays on chip and in L2)
+    # refinement 1.04 KB per candidate (its data stays on chip and in L2)
     traffic = None
     if top == "refine":
-        traffic = 2.4e3 * float(np.sum(r["ncand"]))
+        traffic = 1.04e3 * float(np.sum(r["ncand"]))
     roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_src,
             "kernel_ms_per_launch": top_ms,
