@@ -786,41 +786,55 @@ __device__ __forceinline__ void compose_affine(const double *sRn, double *sRb, c
 // column j.
 template <typename DT, typename KT, typename DF>
 __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, const DF &dist) {
+    // sift-up and sift-down move a hole instead of swapping: the same
+    // comparisons and the same final array as element swaps, one store each
     for (int j = 0; j < m; ++j) {
-        hd[j] = dist(j);
-        hk[j] = (KT)j;
+        const DT d = dist(j);
         int l = j + 1;
         while (l > 1) {
-            int l2 = l / 2;
-            if (hd[l2 - 1] < hd[l - 1]) {
-                DT h = hd[l2 - 1]; hd[l2 - 1] = hd[l - 1]; hd[l - 1] = h;
-                KT t = hk[l2 - 1]; hk[l2 - 1] = hk[l - 1]; hk[l - 1] = t;
-                l = l2;
-            } else break;
+            const int l2 = l / 2;
+            const DT p = hd[l2 - 1];
+            if (!(p < d)) break;
+            hd[l - 1] = p;
+            hk[l - 1] = hk[l2 - 1];
+            l = l2;
         }
+        hd[l - 1] = d;
+        hk[l - 1] = (KT)j;
     }
+    DT root = hd[0];
     for (int j = m; j < ns; ++j) {
-        DT d = dist(j);
-        if (!(d < hd[0])) continue;
-        hd[0] = d;
-        hk[0] = (KT)j;
+        const DT d = dist(j);
+        if (!(d < root)) continue;
+        DT nroot = d;
         int l = 1;
         for (int guard = 0; guard < 64; ++guard) {
-            int l2 = 2 * l;
+            const int l2 = 2 * l;
             if (l2 + 1 > m) {
-                if (l2 <= m && hd[l2 - 1] > hd[l - 1]) {
-                    DT h = hd[l2 - 1]; hd[l2 - 1] = hd[l - 1]; hd[l - 1] = h;
-                    KT t = hk[l2 - 1]; hk[l2 - 1] = hk[l - 1]; hk[l - 1] = t;
+                if (l2 <= m) {
+                    const DT c = hd[l2 - 1];
+                    if (c > d) {
+                        hd[l - 1] = c;
+                        hk[l - 1] = hk[l2 - 1];
+                        if (l == 1) nroot = c;
+                        l = l2;
+                    }
                 }
                 break;
             }
-            int a = (hd[l2] > hd[l2 - 1]) ? l2 + 1 : l2;
-            if (hd[a - 1] > hd[l - 1]) {
-                DT h = hd[a - 1]; hd[a - 1] = hd[l - 1]; hd[l - 1] = h;
-                KT t = hk[a - 1]; hk[a - 1] = hk[l - 1]; hk[l - 1] = t;
-                l = a;
-            } else break;
+            const DT c0 = hd[l2 - 1], c1 = hd[l2];
+            const bool right = c1 > c0;
+            const int a = right ? l2 + 1 : l2;
+            const DT ca = right ? c1 : c0;
+            if (!(ca > d)) break;
+            hd[l - 1] = ca;
+            hk[l - 1] = hk[a - 1];
+            if (l == 1) nroot = ca;
+            l = a;
         }
+        hd[l - 1] = d;
+        hk[l - 1] = (KT)j;
+        root = nroot;
     }
 }
 
