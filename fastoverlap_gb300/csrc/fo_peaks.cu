@@ -145,8 +145,11 @@ __device__ __forceinline__ void warp_reduce77(const T (&h)[77], T *out) {
 
 // Damped normal equations (H + lambda diag(H)) dl = -g, H packed in Hg[0..65]
 // and g in Hg[66..76], solved by Cholesky in registers; in FP32 after scaling
-// the system to unit diagonal, which leaves the step unchanged.  Returns false
-// when the matrix is not positive definite (dl is then meaningless).
+// the system to unit diagonal, which leaves the step unchanged.  The FP32
+// scale factors and pivot reciprocals come from the hardware reciprocal
+// square root (a step's direction, not its acceptance, depends on them).
+// Returns false when the matrix is not positive definite (dl is then
+// meaningless).
 template <typename T>
 __device__ __forceinline__ bool lm_solve(const T *Hg, T lambda, T (&dl)[11]) {
     constexpr bool kScale = sizeof(T) == 4;
@@ -154,7 +157,8 @@ __device__ __forceinline__ bool lm_solve(const T *Hg, T lambda, T (&dl)[11]) {
 #pragma unroll
     for (int a = 0; a < 11; ++a) {
         const T dgl = Hg[a * (a + 1) / 2 + a];
-        sc[a] = kScale ? T(1) / sqrt(dgl > T(1e-30) ? dgl : T(1e-30)) : T(1);
+        if constexpr (kScale) sc[a] = rsqrtf(dgl > T(1e-30) ? dgl : T(1e-30));
+        else sc[a] = T(1);
     }
 #pragma unroll
     for (int a = 0; a < 11; ++a)
@@ -173,9 +177,12 @@ __device__ __forceinline__ bool lm_solve(const T *Hg, T lambda, T (&dl)[11]) {
 #pragma unroll
         for (int k = 0; k < j; ++k) s -= A[jj + k] * A[jj + k];
         ok = ok && (s > T(0));
-        const T djj = sqrt(s > T(0) ? s : T(1));
-        inv[j] = T(1) / djj;
-        A[jj + j] = djj;
+        if constexpr (kScale) {
+            inv[j] = rsqrtf(s > T(0) ? s : T(1));
+        } else {
+            const T djj = sqrt(s > T(0) ? s : T(1));
+            inv[j] = T(1) / djj;
+        }
 #pragma unroll
         for (int i = j + 1; i < 11; ++i) {
             const int ii = i * (i + 1) / 2;
