@@ -545,7 +545,10 @@ __device__ __forceinline__ void warp_halve(double *v, int lane) {
 
 // Cyclic Jacobi rotations (Golub & Van Loan 8.5) on a symmetric 4x4 FP32
 // matrix scaled to unit largest element; a sweep in which every off-diagonal
-// element is at most 2^-22 ends it.  Columns of V are the eigenvectors.
+// element is at most 2^-22 ends it.  Columns of V are the eigenvectors.  The
+// rotation angles use the hardware reciprocal and reciprocal square root: the
+// result only starts the FP64 correction, and every rotation is orthogonal
+// to FP32 rounding whatever its angle.
 __device__ __forceinline__ void jacobi4f(float (&a)[4][4], float (&V)[4][4]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -560,9 +563,11 @@ __device__ __forceinline__ void jacobi4f(float (&a)[4][4], float (&V)[4][4]) {
                 const float apr = a[p][r];
                 if (fabsf(apr) <= 2.384185791015625e-7f) continue;
                 rotated = true;
-                const float theta = (a[r][r] - a[p][p]) / (2.f * apr);
-                const float t = copysignf(1.f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
-                const float c = 1.f / sqrtf(fmaf(t, t, 1.f)), s = t * c;
+                // |apr| > 2^-22 and |a| <= ~2 keep |theta| below 2^23
+                const float theta = __fdividef(a[r][r] - a[p][p], 2.f * apr);
+                const float th2 = fmaf(theta, theta, 1.f);
+                const float t = __fdividef(copysignf(1.f, theta), fabsf(theta) + th2 * rsqrtf(th2));
+                const float c = rsqrtf(fmaf(t, t, 1.f)), s = t * c;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const float akp = a[k][p], akr = a[k][r];
