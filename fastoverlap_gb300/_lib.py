@@ -117,6 +117,10 @@ EXPORTS = {
     "fo_bulk_align": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
+    "fo_bulk_align_group": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int]),
     "fo_bulk_calcdefaults": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, _dp, _ip, _ip]),
     "fo_profile_kernels": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_char_p), _dp, _ip,

@@ -1084,6 +1084,72 @@ fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natom
     return FO_OK;
 }
 
+// ALIGNGROUP: pair (i, j) is ALIGN of structure j of list 2 onto structure i
+// of list 1 with the same parameters, so the pairs run as bulk batches
+// (chunks bound the host and device staging).  With sym only i >= j are
+// aligned, as the reference's triangular loop does.
+fo_status fo_bulk_align_group(fo_ctx *ctx, const double *coords1list, int n1list, const double *coords2list,
+                              int n2list, int natoms, int debug, double boxlx, double boxly, double boxlz,
+                              double kwidth, int ndisplacements, int nwave, int nfspace, double *distmat,
+                              double *alignedcoords2, int sym) {
+    (void)debug;
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    if (!coords1list || !coords2list || !distmat || natoms < 1 || n1list < 1 || n2list < 1)
+        return set_err(ctx, FO_ERR_BAD_ARGS, "null argument or empty list");
+    if (sym && n2list > n1list) return set_err(ctx, FO_ERR_BAD_ARGS, "sym needs n2list <= n1list");
+    std::vector<int> perm, sizes;
+    current_groups(ctx, natoms, perm, sizes);
+    const size_t per = 3 * (size_t)natoms;
+    std::vector<std::pair<int, int>> todo;
+    for (int j = 0; j < n2list; ++j)
+        for (int i = sym ? j : 0; i < n1list; ++i) todo.emplace_back(i, j);
+    for (size_t k = 0; k < (size_t)n1list * n2list; ++k) distmat[k] = 0.0;
+    if (alignedcoords2) memset(alignedcoords2, 0, (size_t)n1list * n2list * per * sizeof(double));
+    // about 64 MiB of coordinates per side and at most 4096 pairs per batch
+    const size_t chunk = std::max<size_t>(1, std::min<size_t>(4096, ((size_t)8 << 20) / per));
+    std::vector<double> p1, p2, al;
+    std::vector<int> pb;
+    std::vector<fo_bulk_pair> q;
+    std::vector<fo_pair_result> res;
+    for (size_t c0 = 0; c0 < todo.size(); c0 += chunk) {
+        const size_t nb = std::min(chunk, todo.size() - c0);
+        p1.resize(nb * per);
+        p2.resize(nb * per);
+        al.resize(nb * per);
+        pb.resize(nb * natoms);
+        q.assign(nb, fo_bulk_pair{});
+        res.assign(nb, fo_pair_result{});
+        for (size_t k = 0; k < nb; ++k) {
+            const int i = todo[c0 + k].first, j = todo[c0 + k].second;
+            memcpy(&p1[k * per], coords1list + (size_t)i * per, per * sizeof(double));
+            memcpy(&p2[k * per], coords2list + (size_t)j * per, per * sizeof(double));
+            fo_bulk_pair &b = q[k];
+            b.natoms = natoms;
+            b.ngroups = (int)sizes.size();
+            b.nwave = nwave;
+            b.nfspace = nfspace;
+            b.ndisps = ndisplacements;
+            b.sigma = kwidth;
+            b.box[0] = boxlx;
+            b.box[1] = boxly;
+            b.box[2] = boxlz;
+            b.coord_off = (int64_t)(k * natoms);
+        }
+        fo_status s = fo_bulk_align_batch(ctx, (int)nb, q.data(), p1.data(), p2.data(), perm.data(), sizes.data(),
+                                          1, al.data(), pb.data(), res.data());
+        if (s) return s;
+        for (size_t k = 0; k < nb; ++k) {
+            if (res[k].status) return set_err(ctx, (fo_status)res[k].status, "pair (%d, %d): %s",
+                                              todo[c0 + k].first + 1, todo[c0 + k].second + 1,
+                                              fo_status_string((fo_status)res[k].status));
+            const size_t ij = (size_t)todo[c0 + k].first + (size_t)n1list * todo[c0 + k].second;
+            distmat[ij] = res[k].dist;
+            if (alignedcoords2) memcpy(alignedcoords2 + ij * per, &al[k * per], per * sizeof(double));
+        }
+    }
+    return FO_OK;
+}
+
 fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz, double *kernelwidth,
                                int *nwave, int *nfspace) {
     if (natoms < 1 || !kernelwidth || !nwave || !nfspace) return FO_ERR_BAD_ARGS;
@@ -1092,7 +1158,13 @@ fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double bo
     int nw = (int)std::ceil(2 * 3.14159265359 / std::min(boxlx, std::min(boxly, boxlz)) * maxk);
     *kernelwidth = kw;
     *nwave = nw;
-    *nfspace = fastlen(4 * nw + 3);
+    if (2 * nw + 1 <= 200) {
+        *nfspace = fastlen(4 * nw + 3);
+    } else {   // the next power of two
+        int m = 1;
+        while (m < 4 * nw + 3) m *= 2;
+        *nfspace = m;
+    }
     return FO_OK;
 }
 

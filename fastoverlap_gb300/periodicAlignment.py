@@ -1,11 +1,14 @@
 """Periodic (bulk) alignment classes with the upstream signatures.
 
 Drop-in for fastoverlap/periodicAlignment.py's `PeriodicAlign` (:341-479)
-and `PeriodicAlignFortran` (:482-605).  Both run the GPU pipeline of the
+and `PeriodicAlignFortran` (:482-605), group alignment included
+(`alignGroup`, :462-479 and :570-605 / fastbulk.f90 ALIGNGROUP :336-412).  Both run the GPU pipeline of the
 Fortran bulk path (fastbulk.f90 ALIGN/ALIGN1): structure factors, damped
 cross product, 3-D FFT, peak fits, iterative permutation/displacement
 refinement from every peak.
 """
+import ctypes
+
 import numpy as np
 
 from . import _lib
@@ -69,6 +72,37 @@ class PeriodicAlign(object):
         X2 = self.periodic(pos2[perm] - disp[None, :], True)
         return float(r["dist"]), X1, X2, perm, disp
 
+    def alignGroup(self, coords, keepCoords=False, npeaks=1, width=2, chunk=4096):
+        """Every structure of `coords` aligned onto every other, as
+        periodicAlignment.py:462-479: dists[i, j] = align(coords[i],
+        coords[j])[0]; with keepCoords also aligned[0, i, j] = X1 and
+        aligned[1, i, j] = X2.  All pairs run as periodic batches of at most
+        `chunk` pairs; `width` is taken as align takes it (the peak search
+        starts at half-width 2 and widens)."""
+        coords = [np.asarray(p, float).reshape(-1, 3) for p in coords]
+        n = len(coords)
+        dists = np.zeros((n, n))
+        aligned = np.empty((2, n, n) + coords[0].shape) if keepCoords else None
+        pairs = [(i, j) for i in range(n) for j in range(n)]
+        for c0 in range(0, len(pairs), chunk):
+            part = pairs[c0:c0 + chunk]
+            b = BulkBatch(self.ctx, [coords[i] for i, _ in part], [coords[j] for _, j in part],
+                          self.boxvec, [self.perm] * len(part), scale=self.scale, nwave=self.n,
+                          nfspace=0, ndisps=max(1, int(npeaks)))
+            out = b.run()
+            for k, (i, j) in enumerate(part):
+                r = out["result"][k]
+                if r["status"] != 0:
+                    raise _lib.FoError(int(r["status"]), "periodic alignment of (%d, %d) failed" % (i, j))
+                dists[i, j] = r["dist"]
+                if keepCoords:
+                    disp = -np.asarray(r["disp"], float)
+                    aligned[0, i, j] = self.periodic(coords[i], True)
+                    aligned[1, i, j] = self.periodic(coords[j][out["perm"][k]] - disp[None, :], True)
+        if keepCoords:
+            return dists, aligned
+        return dists
+
     def __call__(self, pos1, pos2, *args, **kwargs):
         return self.align(pos1, pos2, *args, **kwargs)
 
@@ -123,6 +157,38 @@ class PeriodicAlignFortran(object):
         if r["status"] != 0:
             raise _lib.FoError(int(r["status"]), "periodic alignment failed")
         return float(r["dist"]), pos1.copy(), out["aligned"][0].copy(), out["perm"][0].copy()
+
+    def alignGroup(self, coords, ndisps=1):
+        """Aligns a list of coordinates with themselves through
+        fo_bulk_align_group (BULKFASTOVERLAP::ALIGNGROUP with SYM, as
+        periodicAlignment.py:570-605 calls it).  The Gaussian width, K and M
+        come from CALCDEFAULTS whatever `scale` is, as there.
+
+        Returns dists (nlist, nlist): [i, j] for i >= j is structure j aligned
+        onto structure i, the other entries 0; and aligned
+        (Natoms, 3, nlist, nlist)."""
+        coordslist = np.asarray(coords, dtype=float)
+        nlist, natoms, dim = coordslist.shape
+        assert dim == 3
+        assert natoms == self.Natoms
+        lib = self.ctx.lib
+        kw, nw, nf = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        bx, by, bz = (float(v) for v in self.boxvec)
+        self.ctx.check(lib.fo_bulk_calcdefaults(natoms, bx, by, bz, ctypes.byref(kw), ctypes.byref(nw),
+                                                ctypes.byref(nf)), "calcdefaults")
+        pg = np.ascontiguousarray(self.permgroup, dtype=np.int32)
+        ns = np.ascontiguousarray(self.npermsize, dtype=np.int32)
+        self.ctx.check(lib.fo_setperm(self.ctx.h, natoms, _lib.i(pg), _lib.i(ns), len(ns)), "setperm")
+        flat = np.ascontiguousarray(coordslist.reshape(nlist, 3 * natoms))   # (3N, nlist) column-major
+        dist = np.zeros(nlist * nlist)
+        al = np.zeros(nlist * nlist * 3 * natoms)
+        st = lib.fo_bulk_align_group(self.ctx.h, _lib.d(flat), nlist, _lib.d(flat), nlist, natoms, 0,
+                                     bx, by, bz, kw.value, int(ndisps), nw.value, nf.value,
+                                     _lib.d(dist), _lib.d(al), 1)
+        self.ctx.check(st, "align group")
+        dists = dist.reshape(nlist, nlist, order="F")
+        aligned = al.reshape(3 * natoms, nlist, nlist, order="F").reshape(natoms, 3, nlist, nlist)
+        return dists, aligned
 
     def __call__(self, pos1, pos2, *args, **kwargs):
         return self.align(pos1, pos2, *args, **kwargs)

@@ -17,6 +17,8 @@
  *                             and ALIGN1 (:414-499) when nwave/nfspace are given
  *                             (f2py bulkfastoverlap.align, periodicAlignment.py:562-565)
  *   fo_bulk_calcdefaults   <- BULKFASTOVERLAP::CALCDEFAULTS fastoverlap/f90/fastbulk.f90:253-277
+ *   fo_bulk_align_group    <- BULKFASTOVERLAP::ALIGNGROUP fastoverlap/f90/fastbulk.f90:336-412
+ *                             (f2py bulkfastoverlap.aligngroup, periodicAlignment.py:570-605)
  *   fo_cluster_align_batch <- SphericalAlign.__call__ / SphericalAlignFortran.__call__
  *                             applied to many pairs (sphericalAlignment.py:237-247,491-533)
  *   fo_bulk_align_batch    <- PeriodicAlignFortran.align applied to many pairs
@@ -232,6 +234,20 @@ fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natom
                         int debug, double boxlx, double boxly, double boxlz,
                         double kwidth, int ndisplacements, int nwave, int nfspace,
                         double *distance, double *dist2);
+
+/* BULKFASTOVERLAP::ALIGNGROUP: structure j of coords2list aligned onto
+ * structure i of coords1list for every (i, j) -- or, with sym, for i >= j
+ * only, the list-2 structures standing for list 1's (the reference reuses
+ * list 1's coefficients there).  Fortran (column-major) layouts:
+ * coords1list(3*natoms, n1list), coords2list(3*natoms, n2list),
+ * distmat(n1list, n2list), alignedcoords2(3*natoms, n1list, n2list) (may be
+ * NULL); entries sym skips are 0.  The groups are those of fo_setperm; every
+ * pair runs as ALIGN / ALIGN1 with the given parameters. */
+fo_status fo_bulk_align_group(fo_ctx *ctx, const double *coords1list, int n1list,
+                              const double *coords2list, int n2list, int natoms, int debug,
+                              double boxlx, double boxly, double boxlz, double kwidth,
+                              int ndisplacements, int nwave, int nfspace, double *distmat,
+                              double *alignedcoords2, int sym);
 
 /* BULKFASTOVERLAP::CALCDEFAULTS */
 fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz,
