@@ -1190,6 +1190,168 @@ int orc_cluster_align(const double *pos1, const double *pos2, int n,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Harmonic-oscillator basis (HARMONICNL fastclusters.f90:492-540): the
+ * overlap integral of the Gaussian kernel at distance rj with the basis
+ * function of order (i, j), by the recurrence in i that starts from the
+ * closed form at i = 0.                                                    */
+void orc_harmonic_nl(int nmax, int lmax, double rj, double sigma, double r0, double *ret) {
+    const int w = lmax + 1;
+    memset(ret, 0, sizeof(double) * (size_t)(nmax + 1) * w);
+    double rs = 1.0 / (r0 * r0 + sigma * sigma);
+    ret[0] = sqrt(2.0 * sqrt(ORC_PI) * pow(r0 * rs, 3)) * sigma * sigma * sigma * exp(-0.5 * rj * rj * rs) * 4 * ORC_PI;
+    const double f = sqrt(2.0) * r0 * rj * rs;
+    for (int j = 1; j <= lmax; ++j) ret[j] = f / sqrt(1.0 + 2.0 * j) * ret[j - 1];
+    const double q = sigma * sigma / rj / r0;
+    if (nmax >= 1)
+        for (int j = 0; j <= lmax - 2; ++j)
+            ret[w + j] = sqrt(1 + j + 0.5) * ret[j] - (2.0 * j + 3.0) * q * ret[j + 1] - sqrt(1 + j + 1.5) * ret[j + 2];
+    for (int i = 2; i <= nmax; ++i) {
+        const double si = sqrt((double)i);
+        for (int j = 0; j <= lmax - 2 * i; ++j)
+            ret[i * w + j] = (sqrt(i + j + 0.5) * ret[(i - 1) * w + j] - (2.0 * j + 3.0) * q * ret[(i - 1) * w + j + 1] -
+                              sqrt(i + j + 1.5) * ret[(i - 1) * w + j + 2] + sqrt(i - 1.0) * ret[(i - 2) * w + j + 2]) / si;
+    }
+}
+
+/* HARMONICCOEFFS (fastclusters.f90:654-687): c_nlm = sum_atoms d_nl conj(Y_lm),
+ * d from HARMONICNL with lmax = L + 2 nmax.                                */
+void orc_harmonic_coeffs(const double *X, int natoms, int nmax, int L, double hwidth,
+                         double kwidth, double *cnml) {
+    const int W = 2 * L + 1, lw = L + 2 * nmax + 1;
+    memset(cnml, 0, sizeof(double) * 2 * (size_t)(nmax + 1) * (L + 1) * W);
+    double *yr = malloc(sizeof(double) * (L + 1) * W), *yi = malloc(sizeof(double) * (L + 1) * W);
+    double *d = malloc(sizeof(double) * (size_t)(nmax + 1) * lw);
+    for (int k = 0; k < natoms; ++k) {
+        const double *x = X + 3 * k;
+        orc_ylm(x, L, yr, yi);
+        orc_harmonic_nl(nmax, L + 2 * nmax, sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]), kwidth, hwidth, d);
+        for (int l = 0; l <= L; ++l)
+            for (int m = -l; m <= l; ++m) {
+                const double ar = yr[l * W + L + m], ai = yi[l * W + L + m];
+                const int im = (m + W) % W;
+                for (int i = 0; i <= nmax; ++i) {
+                    double *c = cnml + 2 * (((size_t)i * (L + 1) + l) * W + im);
+                    c[0] += d[i * lw + l] * ar;
+                    c[1] -= d[i * lw + l] * ai;
+                }
+            }
+    }
+    free(yr); free(yi); free(d);
+}
+
+/* DOTHARMONICCOEFFS (fastclusters.f90:740-759), added into the ilmm layout */
+void orc_dot_harmonic(const double *c1, const double *c2, int nmax, int L, double *ilmm) {
+    const int W = 2 * L + 1;
+    for (int l = 0; l <= L; ++l)
+        for (int m1 = -l; m1 <= l; ++m1)
+            for (int m2 = -l; m2 <= l; ++m2) {
+                const int i1 = (m1 + W) % W, i2 = (m2 + W) % W;
+                double re = 0, im = 0;
+                for (int i = 0; i <= nmax; ++i) {
+                    const double *a = c1 + 2 * (((size_t)i * (L + 1) + l) * W + i1);
+                    const double *b = c2 + 2 * (((size_t)i * (L + 1) + l) * W + i2);
+                    re += a[0] * b[0] + a[1] * b[1];   /* conj(a) b */
+                    im += a[0] * b[1] - a[1] * b[0];
+                }
+                double *o = ilmm + 2 * (((size_t)l * W + i1) * W + i2);
+                o[0] += re;
+                o[1] += im;
+            }
+}
+
+/* IMML = sum over groups of DOTHARMONICCOEFFS(coefficients of B's group,
+ * coefficients of sign_a * A's group); parity (-1)^l for the inversion is
+ * the same as negating A.                                                  */
+static void orc_harm_groups(const double *B, const double *A, int n, const int *perm, const int *gsize,
+                            int ngroups, int nmax, int L, double hwidth, double kwidth, double sign_a,
+                            double *ilmm) {
+    const int W = 2 * L + 1;
+    const size_t nc = 2 * (size_t)(nmax + 1) * (L + 1) * W;
+    memset(ilmm, 0, sizeof(double) * 2 * (size_t)(L + 1) * W * W);
+    double *cb = malloc(sizeof(double) * nc), *ca = malloc(sizeof(double) * nc);
+    double *pb = malloc(sizeof(double) * 3 * (n ? n : 1)), *pa = malloc(sizeof(double) * 3 * (n ? n : 1));
+    int off = 0;
+    for (int g = 0; g < ngroups; ++g) {
+        const int ns = gsize[g];
+        for (int j = 0; j < ns; ++j)
+            for (int k = 0; k < 3; ++k) {
+                pb[3 * j + k] = B[3 * perm[off + j] + k];
+                pa[3 * j + k] = A[3 * perm[off + j] + k];
+            }
+        orc_harmonic_coeffs(pb, ns, nmax, L, hwidth, kwidth, cb);
+        orc_harmonic_coeffs(pa, ns, nmax, L, hwidth, kwidth, ca);
+        if (sign_a < 0)
+            for (int i = 0; i <= nmax; ++i)
+                for (int l = 1; l <= L; l += 2)
+                    for (int m = 0; m < 2 * W; ++m) ca[2 * (((size_t)i * (L + 1) + l) * W) + m] *= -1.0;
+        orc_dot_harmonic(cb, ca, nmax, L, ilmm);
+        off += ns;
+    }
+    free(cb); free(ca); free(pb); free(pa);
+}
+
+/* ALIGNHARM (fastclusters.f90:271-391) with ALIGN's coordinate handling (see
+ * the header): coefficients of the coordinates as given, ALIGNCOEFFS, and
+ * with invert the same for -A, the smaller distance winning (ties: the
+ * non-inverted alignment).                                                 */
+int orc_harm_align(const double *pos1, const double *pos2, int n, const int *perm, const int *gsize,
+                   int ngroups, int nmax, int L, double hwidth, double kwidth, int nrot, int invert,
+                   double *aligned, int *permbest, orc_result *res) {
+    memset(res, 0, sizeof *res);
+    res->sigma = kwidth;
+    const int W = 2 * L + 1;
+    double *ilmm = malloc(sizeof(double) * 2 * (size_t)(L + 1) * W * W);
+    orc_harm_groups(pos1, pos2, n, perm, gsize, ngroups, nmax, L, hwidth, kwidth, 1.0, ilmm);
+    double *al = malloc(sizeof(double) * 3 * n), *Ainv = malloc(sizeof(double) * 3 * n);
+    int *pb = malloc(sizeof(int) * n);
+    double Rb[9], dist, omax;
+    int rc = orc_align_coeffs(pos1, pos2, n, perm, gsize, ngroups, L, ilmm, nrot, aligned, permbest, res->rmat,
+                              &res->dist, &res->overlap_max, &res->ncand);
+    if (rc == 0 && invert) {
+        for (int j = 0; j < 3 * n; ++j) Ainv[j] = -pos2[j];
+        orc_harm_groups(pos1, pos2, n, perm, gsize, ngroups, nmax, L, hwidth, kwidth, -1.0, ilmm);
+        rc = orc_align_coeffs(pos1, Ainv, n, perm, gsize, ngroups, L, ilmm, nrot, al, pb, Rb, &dist, &omax,
+                              &res->ncand);
+        if (rc == 0 && dist < res->dist) {
+            res->dist = dist;
+            memcpy(aligned, al, sizeof(double) * 3 * n);
+            memcpy(permbest, pb, sizeof(int) * n);
+            memcpy(res->rmat, Rb, sizeof Rb);
+            res->inverted = 1;
+            res->overlap_max = omax;
+        }
+    }
+    res->status = rc;
+    free(ilmm); free(al); free(Ainv); free(pb);
+    return rc;
+}
+
+/* CALCSIMILARITY (fastclusters.f90:790-815): IMML summed over the groups,
+ * its squared norm, and the maximum of the overlap grid CALCOVERLAP forms. */
+void orc_calc_similarity(const double *c1, const double *c2, int ngroups, int nmax, int L, double *norm,
+                         double *maxover) {
+    const int W = 2 * L + 1, G = 2 * (L + 1);
+    const size_t nc = 2 * (size_t)(nmax + 1) * (L + 1) * W, ni = 2 * (size_t)(L + 1) * W * W;
+    double *ilmm = calloc(ni, sizeof(double));
+    for (int g = 0; g < ngroups; ++g) orc_dot_harmonic(c1 + g * nc, c2 + g * nc, nmax, L, ilmm);
+    double s = 0;
+    for (int l = 0; l <= L; ++l)
+        for (int m1 = -l; m1 <= l; ++m1)
+            for (int m2 = -l; m2 <= l; ++m2) {
+                const double *o = ilmm + 2 * (((size_t)l * W + (m1 + W) % W) * W + (m2 + W) % W);
+                s += o[0] * o[0] + o[1] * o[1];
+            }
+    *norm = s;
+    double *grid = malloc(sizeof(double) * (size_t)G * G * G);
+    orc_isoft(L + 1, ilmm, grid);
+    double mx = grid[0];
+    for (size_t i = 1; i < (size_t)G * G * G; ++i)
+        if (grid[i] > mx) mx = grid[i];
+    *maxover = mx;
+    free(grid); free(ilmm);
+}
+
+/* ------------------------------------------------------------------------ */
 /* SETWAVEK / PERIODICFOURIERPERM / damping / DOTFOURIERCOEFFS / FFT3D / ABS
  * (fastbulk.f90:414-454,522-523,567-683; fastutils.f90:554-569):
  *   F(k) = sum_s C^B_s(k) conj(C^A_s(k)) exp(-k^2 s^2),

@@ -85,6 +85,32 @@ int    orc_bulk_align(const double *pos1, const double *pos2, int n,
                       const double box[3], double sigma, int nwave, int nfspace,
                       int ndisps, double *aligned, int *permbest, orc_result *res);
 
+/* Harmonic-oscillator basis (the SphericalHarmonicAlignFortran path).
+ * HARMONICNL fastoverlap/f90/fastclusters.f90:492-540: ret[i*(lmax+1)+j],
+ * i <= nmax, j <= lmax - 2i (j <= lmax - 2 for i = 1).                    */
+void   orc_harmonic_nl(int nmax, int lmax, double rj, double sigma, double r0, double *ret);
+/* HARMONICCOEFFS :654-687 (coordinates as given, not centred):
+ * cnml[((n*(L+1) + l)*W + m mod W)] complex interleaved, W = 2L+1.        */
+void   orc_harmonic_coeffs(const double *X, int natoms, int nmax, int L, double hwidth,
+                           double kwidth, double *cnml);
+/* DOTHARMONICCOEFFS :740-759 added into ilmm:
+ * IMML(m1,m2,l) += sum_n conj(c1(n,m1,l)) c2(n,m2,l).                     */
+void   orc_dot_harmonic(const double *c1, const double *c2, int nmax, int L, double *ilmm);
+/* ALIGNHARM :271-391: per-group harmonic coefficients of the coordinates
+ * as given, ALIGNCOEFFS, then (invert) the same for -A.  The refinement
+ * takes the coordinates in their own order and the inverted winner keeps
+ * its own rotation, as ALIGN does (ALIGNHARM leaves its per-group copies
+ * in place and returns the non-inverted rotation; the two agree for one
+ * permutation group in index order and for non-inverted winners).         */
+int    orc_harm_align(const double *pos1, const double *pos2, int n,
+                      const int *perm, const int *gsize, int ngroups, int nmax, int L,
+                      double hwidth, double kwidth, int nrot, int invert,
+                      double *aligned, int *permbest, orc_result *res);
+/* CALCSIMILARITY :790-815 over stacked per-group coefficients
+ * c[g][n][l][m]: norm = sum |IMML|^2, maxover = max of the overlap grid.    */
+void   orc_calc_similarity(const double *c1, const double *c2, int ngroups, int nmax, int L,
+                           double *norm, double *maxover);
+
 /* batch helper for the CPU baseline: runs pairs on nthreads OS threads */
 int    orc_cluster_align_many(int npairs, const double *pos1, const double *pos2,
                               const int64_t *coord_off, const int *natoms,

@@ -50,6 +50,7 @@ def lib():
         _LIB.orc_jv.restype = ctypes.c_int
         _LIB.orc_cluster_align.restype = ctypes.c_int
         _LIB.orc_bulk_align.restype = ctypes.c_int
+        _LIB.orc_harm_align.restype = ctypes.c_int
     return _LIB
 
 
@@ -204,6 +205,70 @@ def cluster_align(pos1, pos2, perm=None, Jmax=15, sigma=0.3, nrot=10, invert=Tru
     return dict(status=rc, dist=r.dist, aligned=al, perm=pb,
                 rmat=np.array(r.rmat).reshape(3, 3), inverted=bool(r.inverted),
                 ncand=r.ncand, sigma=r.sigma, overlap_max=r.overlap_max)
+
+
+def harmonic_nl(nmax, lmax, rj, sigma, r0):
+    """HARMONICNL: (nmax+1, lmax+1) overlap integrals of one kernel."""
+    out = np.zeros((nmax + 1) * (lmax + 1))
+    lib().orc_harmonic_nl(int(nmax), int(lmax), ctypes.c_double(rj), ctypes.c_double(sigma),
+                          ctypes.c_double(r0), _d(out))
+    return out.reshape(nmax + 1, lmax + 1)
+
+
+def harmonic_coeffs(X, nmax, L, hwidth, kwidth):
+    """HARMONICCOEFFS of the coordinates as given: complex (nmax+1, L+1, 2L+1)
+    indexed [n, l, m mod (2L+1)] (the upstream Python calcHarmCoeff layout)."""
+    X = np.ascontiguousarray(X, dtype=np.float64).reshape(-1, 3)
+    W = 2 * L + 1
+    out = np.zeros(2 * (nmax + 1) * (L + 1) * W)
+    lib().orc_harmonic_coeffs(_d(X), len(X), int(nmax), int(L), ctypes.c_double(hwidth),
+                              ctypes.c_double(kwidth), _d(out))
+    return (out[0::2] + 1j * out[1::2]).reshape(nmax + 1, L + 1, W)
+
+
+def harm_align(pos1, pos2, perm=None, nmax=20, Jmax=15, hwidth=1.0, kwidth=0.3, nrot=10,
+               invert=True):
+    """ALIGNHARM semantics (coordinates as given).  Returns dict of outputs."""
+    p1 = np.ascontiguousarray(pos1, dtype=np.float64).reshape(-1, 3)
+    p2 = np.ascontiguousarray(pos2, dtype=np.float64).reshape(-1, 3)
+    n = len(p1)
+    flat, sizes = _groups(perm, n)
+    al = np.zeros((n, 3))
+    pb = np.zeros(n, np.int32)
+    r = OrcResult()
+    rc = lib().orc_harm_align(_d(p1), _d(p2), n, _i(flat), _i(sizes), len(sizes), int(nmax), int(Jmax),
+                              ctypes.c_double(hwidth), ctypes.c_double(kwidth), int(nrot),
+                              int(bool(invert)), _d(al), _i(pb), ctypes.byref(r))
+    return dict(status=rc, dist=r.dist, aligned=al, perm=pb,
+                rmat=np.array(r.rmat).reshape(3, 3), inverted=bool(r.inverted),
+                ncand=r.ncand, overlap_max=r.overlap_max)
+
+
+def overlap_matrices(coordslist, perm=None, nmax=20, Jmax=15, hwidth=1.0, kwidth=0.3):
+    """CALCOVERLAPMATRICES: (norms, maxovers), each (nlist, nlist), from the
+    per-group harmonic coefficients of each structure (coordinates as given)."""
+    X = [np.asarray(x, dtype=np.float64).reshape(-1, 3) for x in coordslist]
+    n = len(X[0])
+    flat, sizes = _groups(perm, n)
+    cs = []
+    for x in X:
+        off, parts = 0, []
+        for sz in sizes:
+            idx = flat[off:off + sz]
+            c = harmonic_coeffs(x[idx], nmax, Jmax, hwidth, kwidth)
+            parts.append(np.stack([c.real, c.imag], -1).ravel())
+            off += sz
+        cs.append(np.ascontiguousarray(np.concatenate(parts)))
+    nl = len(X)
+    norms, maxs = np.zeros((nl, nl)), np.zeros((nl, nl))
+    for i in range(nl):
+        for j in range(i, nl):
+            a, b = ctypes.c_double(), ctypes.c_double()
+            lib().orc_calc_similarity(_d(cs[i]), _d(cs[j]), len(sizes), int(nmax), int(Jmax),
+                                      ctypes.byref(a), ctypes.byref(b))
+            norms[i, j] = norms[j, i] = a.value
+            maxs[i, j] = maxs[j, i] = b.value
+    return norms, maxs
 
 
 def bulk_fspace(pos1, pos2, box, perm=None, sigma=0.2, nwave=7, nf=None):

@@ -101,5 +101,38 @@ def main():
     print("c0", np.round(sph_d, 6), "c1", np.round(per_d, 6))
 
 
+def harm(R=None):
+    """harm.npz: the harmonic-basis path (SphericalHarmonicAlign) on centred
+    structures -- coefficients, the SO(3) coefficients of a pair with their
+    norm and overlap maximum (CALCSIMILARITY's two numbers), and end-to-end
+    distances of four seeded 38-atom pairs (nmax 10, Jmax 7)."""
+    R = R or ref_shim.import_reference(os.environ.get("FO_REF_ROOT", "/root/reference"))
+    nmax, L, hw, kw = 6, 5, 1.0, 0.3
+    p = synth.cluster_pair(7, n=20)
+    X = p["pos1"] - p["pos1"].mean(0)
+    Y = p["pos2"] - p["pos2"].mean(0)
+    a = R.sph.SphericalHarmonicAlign(scale=kw, harmscale=hw, nmax=nmax, Jmax=L)
+    cX = a.calcHarmCoeff(X)                      # [n, l, m mod (2L+1)]
+    so3 = a.calcSO3Coeffs(X, Y)                  # [l, m1, m2], pos1 = X
+    grid = a.soft.iSOFT(so3).real
+    norm = float(np.sum(np.abs(so3) ** 2))
+    dists, pairs1, pairs2 = [], [], []
+    for k in range(4):
+        q = synth.cluster_pair(100 + k, n=38)
+        X1, X2 = q["pos1"] - q["pos1"].mean(0), q["pos2"] - q["pos2"].mean(0)
+        b = R.sph.SphericalHarmonicAlign(scale=0.3, harmscale=1.0, nmax=10, Jmax=7)
+        dists.append(float(np.real(b(X1, X2)[0])))
+        pairs1.append(X1)
+        pairs2.append(X2)
+    np.savez(os.path.join(HERE, "harm.npz"), X=X, Y=Y, nmax=nmax, L=L, hwidth=hw, kwidth=kw, coeffs_X=cX,
+             so3=so3, norm=norm, maxover=float(grid.max()), pos1=np.array(pairs1), pos2=np.array(pairs2),
+             dist_nmax10_j7=np.array(dists))
+    print("harm", np.round(dists, 9), norm, float(grid.max()))
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["harm"]:
+        harm()
+    else:
+        main()
+        harm()

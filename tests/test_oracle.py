@@ -170,3 +170,31 @@ def test_findpeaks_recovers_planted_gaussians(oracle_mod, width):
     assert pk.shape == (2, 3)
     np.testing.assert_allclose(pk, centres + 1.0, atol=2e-3)
     np.testing.assert_allclose(am, [2.0, 1.5], rtol=2e-3)
+
+
+# -- harmonic-oscillator basis (SphericalHarmonicAlign / ALIGNHARM) ----------
+
+def test_harmonic_coefficients_match_upstream(oracle_mod, golden):
+    g = golden("harm")
+    nmax, L = int(g["nmax"]), int(g["L"])
+    c = oracle_mod.harmonic_coeffs(g["X"], nmax, L, float(g["hwidth"]), float(g["kwidth"]))
+    assert np.max(np.abs(c - g["coeffs_X"])) <= 1e-12 * np.max(np.abs(g["coeffs_X"]))
+
+
+def test_harmonic_similarity_matches_upstream(oracle_mod, golden):
+    """DOTHARMONICCOEFFS, and CALCSIMILARITY's norm and overlap maximum."""
+    g = golden("harm")
+    nmax, L, hw, kw = int(g["nmax"]), int(g["L"]), float(g["hwidth"]), float(g["kwidth"])
+    norms, maxs = oracle_mod.overlap_matrices([g["X"], g["Y"]], None, nmax, L, hw, kw)
+    assert abs(norms[0, 1] - float(g["norm"])) <= 1e-12 * float(g["norm"])
+    assert abs(maxs[0, 1] - float(g["maxover"])) <= 1e-12 * abs(float(g["maxover"]))
+    assert norms[0, 1] == norms[1, 0] and maxs[0, 1] == maxs[1, 0]
+
+
+def test_harmonic_alignment_matches_upstream(oracle_mod, golden):
+    g = golden("harm")
+    for k in range(len(g["dist_nmax10_j7"])):
+        o = oracle_mod.harm_align(g["pos1"][k], g["pos2"][k], None, nmax=10, Jmax=7, hwidth=1.0,
+                                  kwidth=0.3, nrot=10, invert=True)
+        assert o["status"] == 0
+        assert abs(o["dist"] - g["dist_nmax10_j7"][k]) <= 1e-8 * o["dist"]
