@@ -3,6 +3,8 @@ alignment path.
 
 Public classes keep the upstream names and signatures:
     SphericalAlign, SphericalAlignFortran   (cluster alignment)
+    SphericalHarmonicAlign, SphericalHarmonicAlignFortran
+                                            (cluster alignment, harmonic-oscillator basis)
     PeriodicAlign, PeriodicAlignFortran     (periodic alignment)
 Batched and resident forms:
     align_clusters, align_periodic, ClusterBatch, BulkBatch
@@ -13,11 +15,14 @@ Serving (requests admitted as they arrive, continuous batching):
 All compute runs in libfastoverlap_gb300.so (CUDA); there is no CPU path.
 """
 from ._lib import Context, FoError, default_context, load  # noqa: F401
-from .batch import BulkBatch, ClusterBatch, align_clusters, align_periodic, findpeaks  # noqa: F401
+from .batch import (BulkBatch, ClusterBatch, HarmonicClusterBatch, align_clusters, align_periodic,  # noqa: F401
+                    findpeaks)
 from .serve import Server  # noqa: F401
 from .periodicAlignment import PeriodicAlign, PeriodicAlignFortran  # noqa: F401
-from .sphericalAlignment import SphericalAlign, SphericalAlignFortran  # noqa: F401
+from .sphericalAlignment import (SphericalAlign, SphericalAlignFortran, SphericalHarmonicAlign,  # noqa: F401
+                                 SphericalHarmonicAlignFortran)
 
-__all__ = ["SphericalAlign", "SphericalAlignFortran", "PeriodicAlign", "PeriodicAlignFortran",
+__all__ = ["SphericalAlign", "SphericalAlignFortran", "SphericalHarmonicAlign", "SphericalHarmonicAlignFortran",
+           "HarmonicClusterBatch", "PeriodicAlign", "PeriodicAlignFortran",
            "align_clusters", "align_periodic", "ClusterBatch", "BulkBatch", "findpeaks", "Server", "Context",
            "FoError", "default_context", "load"]

@@ -117,6 +117,15 @@ EXPORTS = {
     "fo_bulk_align": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
+    "fo_cluster_align_harm": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp,
+                                             ctypes.c_int, ctypes.c_int]),
+    "fo_calc_overlap_matrices": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp]),
+    "fo_cluster_harm_align_batch": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip, ctypes.c_int,
+                                                   ctypes.c_int, ctypes.c_double, _dp, _ip, _vp]),
+    "fo_cluster_harm_plan_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip, ctypes.c_int,
+                                                   ctypes.c_int, ctypes.c_double, ctypes.POINTER(_vp)]),
     "fo_bulk_align_group": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_int,

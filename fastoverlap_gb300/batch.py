@@ -73,10 +73,14 @@ class _BatchBase(object):
         aligned = np.zeros(3 * self.pk.natoms_total)
         permbest = np.zeros(self.pk.natoms_total, np.int32)
         res = np.zeros(self.npairs, _lib.RESULT_DTYPE)
-        fn = lib.fo_cluster_align_batch if self.kind == "cluster" else lib.fo_bulk_align_batch
-        st = fn(self.ctx.h, self.npairs, _lib.vp(self.desc), _lib.d(self.pk.pos1),
-                _lib.d(self.pk.pos2), _lib.i(self.pk.perm), _lib.i(self.pk.sizes), 0,
-                _lib.d(aligned), _lib.i(permbest), _lib.vp(res))
+        args = (self.ctx.h, self.npairs, _lib.vp(self.desc), _lib.d(self.pk.pos1), _lib.d(self.pk.pos2),
+                _lib.i(self.pk.perm), _lib.i(self.pk.sizes), 0)
+        if self.kind == "harmonic":
+            st = lib.fo_cluster_harm_align_batch(*args, int(self.nmax), float(self.harmscale), _lib.d(aligned),
+                                                 _lib.i(permbest), _lib.vp(res))
+        else:
+            fn = lib.fo_cluster_align_batch if self.kind == "cluster" else lib.fo_bulk_align_batch
+            st = fn(*args, _lib.d(aligned), _lib.i(permbest), _lib.vp(res))
         self.ctx.check(st, "align batch")
         return self._unpack(res, aligned, permbest)
 
@@ -84,10 +88,13 @@ class _BatchBase(object):
     def plan(self):
         lib = self.ctx.lib
         h = ctypes.c_void_p()
-        fn = lib.fo_cluster_plan_create if self.kind == "cluster" else lib.fo_bulk_plan_create
-        st = fn(self.ctx.h, self.npairs, _lib.vp(self.desc), _lib.d(self.pk.pos1),
-                _lib.d(self.pk.pos2), _lib.i(self.pk.perm), _lib.i(self.pk.sizes), 0,
-                ctypes.byref(h))
+        args = (self.ctx.h, self.npairs, _lib.vp(self.desc), _lib.d(self.pk.pos1), _lib.d(self.pk.pos2),
+                _lib.i(self.pk.perm), _lib.i(self.pk.sizes), 0)
+        if self.kind == "harmonic":
+            st = lib.fo_cluster_harm_plan_create(*args, int(self.nmax), float(self.harmscale), ctypes.byref(h))
+        else:
+            fn = lib.fo_cluster_plan_create if self.kind == "cluster" else lib.fo_bulk_plan_create
+            st = fn(*args, ctypes.byref(h))
         self.ctx.check(st, "plan create")
         self.plan_h = h
         _lib.track("plans", self)
@@ -162,6 +169,19 @@ class ClusterBatch(_BatchBase):
             dsc.perm_off = int(self.pk.perm_off[k])
             dsc.group_off = int(self.pk.group_off[k])
         self.desc = np.frombuffer(desc, dtype=np.uint8).copy()
+
+
+class HarmonicClusterBatch(ClusterBatch):
+    """Cluster pairs in the harmonic-oscillator basis (SphericalHarmonicAlign /
+    ALIGNHARM): coefficients of the coordinates as given, orders n <= nmax at
+    length scale harmscale; `scale` is the kernel width (> 0)."""
+    kind = "harmonic"
+
+    def __init__(self, ctx, pos1, pos2, perms=None, Jmax=15, scale=0.3, nrot=10, invert=True, nmax=20,
+                 harmscale=1.0):
+        super().__init__(ctx, pos1, pos2, perms, Jmax=Jmax, scale=scale, nrot=nrot, invert=invert)
+        self.nmax = int(nmax)
+        self.harmscale = float(harmscale)
 
 
 class BulkBatch(_BatchBase):

@@ -75,6 +75,8 @@ struct fo_plan {
     int npairs = 0, nslots = 0, ncand = 0, ngroups = 0;
     int maxL = 0, maxG = 0, maxgroup = 0, maxn = 0;
     int index_base = 0;
+    int harm_n = -1;         // >= 0: harmonic-oscillator basis of this order
+    size_t harm_d = 0;       // doubles of its radial overlap buffer
     std::vector<fo::PairDev> hp;
     std::vector<fo::GroupDev> hg;
     std::vector<long long> caller_off;  // caller's atom offset per pair
@@ -428,6 +430,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     size_t o_cnit = cv.take<int>(nc), o_cst = cv.take<int>(nc);
     size_t o_res = cv.take<fo_pair_result>(np), o_al = cv.take<double>(3 * (size_t)ns),
            o_pb = cv.take<int>(ns);
+    size_t o_hd = cv.take<double>(pl->harm_d);
     fo_status s = finish_plan_alloc(ctx, pl, cv.off);
     if (s) return s;
     unsigned char *m = pl->dmem;
@@ -465,6 +468,8 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     pl->sb.maxL = pl->maxL;
     pl->sb.maxG = pl->maxG;
     pl->sb.maxgroup = pl->maxgroup;
+    pl->sb.harm_n = pl->harm_n;
+    pl->sb.hd = pl->harm_d ? (double *)P(o_hd) : nullptr;
     pl->d_coef = P(o_coef);
     pl->coef_bytes = coef_n * 2 * T;
     pl->d_fgrid = P(o_fgrid);
@@ -521,11 +526,16 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     return FO_OK;
 }
 
-fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
-                                 const double *pos1, const double *pos2, const int *perm,
-                                 const int *group_sizes, int index_base, fo_plan **out) {
+// harm_n < 0: the Gaussian-kernel coefficients of ALIGN; harm_n >= 0: the
+// harmonic-oscillator basis of ALIGNHARM (order harm_n, length scale harm_r0).
+static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs, const double *pos1,
+                                     const double *pos2, const int *perm, const int *group_sizes, int index_base,
+                                     int harm_n, double harm_r0, fo_plan **out) {
     if (!ctx || !out || npairs <= 0 || !pairs || !pos1 || !pos2 || !perm || !group_sizes)
         return set_err(ctx, FO_ERR_BAD_ARGS, "null argument or npairs <= 0");
+    if (harm_n > fo::kMaxHarmN || (harm_n >= 0 && !(harm_r0 > 0.0)))
+        return set_err(ctx, FO_ERR_BAD_ARGS, "harmonic basis: nmax %d outside [0,%d] or length scale <= 0", harm_n,
+                       fo::kMaxHarmN);
     *out = nullptr;
     cudaSetDevice(ctx->opts.device);
     fo_plan *pl = new fo_plan();
@@ -548,6 +558,7 @@ fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair 
         if (L < 0 || L > kMaxJmax) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: jmax %d outside [0,%d]", i, L, kMaxJmax); }
         if (q.nrot < 1 || q.nrot > kMaxNrot) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: nrot %d outside [1,%d]", i, q.nrot, kMaxNrot); }
         if (!(q.sigma == q.sigma)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: sigma is NaN", i); }
+        if (harm_n >= 0 && !(q.sigma > 0.0)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: the harmonic basis needs sigma > 0", i); }
         std::vector<int> s2o(n);
         fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
                                    index_base, s2o.data());
@@ -572,6 +583,9 @@ fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair 
         P.grid0 = grid_n;
         P.candatom0 = candatom;
         P.sigma = q.sigma;
+        P.harm = harm_n >= 0 ? 1 : 0;
+        P.harm_n = harm_n >= 0 ? harm_n : 0;
+        P.harm_r0 = harm_r0;
         int maxg = 0, off = 0;
         for (int g = 0; g < q.ngroups; ++g) {
             int gn = group_sizes[q.group_off + g];
@@ -623,12 +637,27 @@ fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair 
     fo_status s = ensure_dtabs(ctx, bws);
     if (s) { delete pl; return s; }
     build_buckets(pl, rassign, cand_list);
+    pl->harm_n = harm_n >= 0 ? harm_n : -1;
+    pl->harm_d = harm_n >= 0 ? 2 * (size_t)pl->nslots * (harm_n + 1) * (pl->maxL + 1) : 0;
     s = plan_common_alloc(ctx, pl, hpos1.data(), hpos2.data(), slot2orig, slot2pair, cand2pair,
                           cand_list, ylm_n, w_n, coef_n, grid_n, 0, lap_total);
     if (s) { fo_plan_destroy(pl); return s; }
     pl->sb.dtab = pl->fp32 ? (const void *const *)ctx->d_dtab32 : (const void *const *)ctx->d_dtab64;
     *out = pl;
     return FO_OK;
+}
+
+fo_status fo_cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs, const double *pos1,
+                                 const double *pos2, const int *perm, const int *group_sizes, int index_base,
+                                 fo_plan **out) {
+    return cluster_plan_create(ctx, npairs, pairs, pos1, pos2, perm, group_sizes, index_base, -1, 0.0, out);
+}
+
+fo_status fo_cluster_harm_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs, const double *pos1,
+                                      const double *pos2, const int *perm, const int *group_sizes, int index_base,
+                                      int nmax, double hwidth, fo_plan **out) {
+    if (nmax < 0) return set_err(ctx, FO_ERR_BAD_ARGS, "nmax %d < 0", nmax);
+    return cluster_plan_create(ctx, npairs, pairs, pos1, pos2, perm, group_sizes, index_base, nmax, hwidth, out);
 }
 
 fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs, const double *pos1,
@@ -1148,6 +1177,112 @@ fo_status fo_bulk_align_group(fo_ctx *ctx, const double *coords1list, int n1list
         }
     }
     return FO_OK;
+}
+
+fo_status fo_cluster_harm_align_batch(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs, const double *pos1,
+                                      const double *pos2, const int *perm, const int *group_sizes, int index_base,
+                                      int nmax, double hwidth, double *aligned, int *permbest,
+                                      fo_pair_result *results) {
+    fo_plan *pl = nullptr;
+    fo_status s = fo_cluster_harm_plan_create(ctx, npairs, pairs, pos1, pos2, perm, group_sizes, index_base, nmax,
+                                              hwidth, &pl);
+    if (s) return s;
+    return run_batch(ctx, pl, aligned, permbest, results);
+}
+
+// ALIGNHARM: the coordinates as given (COORDSB is not centred), the
+// harmonic-basis coefficients, then ALIGNCOEFFS and the inversion as ALIGN.
+fo_status fo_cluster_align_harm(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms, int debug, int n, int l,
+                                double hwidth, double kwidth, double *distance, double *dist2, double *rmatbest,
+                                int nrotations, int perminvopt) {
+    (void)debug;
+    if (!ctx || !coordsb || !coordsa || natoms < 1) return FO_ERR_BAD_ARGS;
+    std::vector<int> perm, sizes;
+    current_groups(ctx, natoms, perm, sizes);
+    fo_cluster_pair q{};
+    q.natoms = natoms;
+    q.ngroups = (int)sizes.size();
+    q.jmax = l;
+    q.nrot = nrotations;
+    q.invert = perminvopt ? 1 : 0;
+    q.sigma = kwidth;
+    std::vector<double> al(3 * (size_t)natoms);
+    std::vector<int> pb(natoms);
+    fo_pair_result r{};
+    fo_status s = fo_cluster_harm_align_batch(ctx, 1, &q, coordsb, coordsa, perm.data(), sizes.data(), 1, n,
+                                              hwidth, al.data(), pb.data(), &r);
+    if (s) return s;
+    if (r.status) return (fo_status)r.status;
+    memcpy(coordsa, al.data(), al.size() * sizeof(double));
+    if (distance) *distance = r.dist;
+    if (dist2) *dist2 = r.dist * r.dist;
+    if (rmatbest)
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) rmatbest[i + 3 * j] = r.rmat[3 * i + j];
+    ctx->bestperm = pb;
+    return FO_OK;
+}
+
+// CALCOVERLAPMATRICES: CALCSIMILARITY of every pair i1 <= i2 (list member i1
+// as the target), mirrored.  The pairs run as harmonic-basis plans through
+// the coefficient and inverse-SOFT stages only.
+fo_status fo_calc_overlap_matrices(fo_ctx *ctx, const double *coordslist, int natoms, int nlist, int n, int l,
+                                   double hwidth, double kwidth, double *norms, double *maxovers) {
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    if (!coordslist || !norms || !maxovers || natoms < 1 || nlist < 1)
+        return set_err(ctx, FO_ERR_BAD_ARGS, "null argument or empty list");
+    cudaSetDevice(ctx->opts.device);
+    std::vector<int> perm, sizes;
+    current_groups(ctx, natoms, perm, sizes);
+    const size_t per = 3 * (size_t)natoms;
+    std::vector<std::pair<int, int>> todo;
+    for (int i1 = 0; i1 < nlist; ++i1)
+        for (int i2 = i1; i2 < nlist; ++i2) todo.emplace_back(i1, i2);
+    const size_t chunk = std::max<size_t>(1, std::min<size_t>(4096, ((size_t)8 << 20) / per));
+    double *d_out = nullptr;
+    fo_status s = cuda_check(ctx, cudaMalloc(&d_out, 2 * chunk * sizeof(double)), "cudaMalloc");
+    if (s) return s;
+    std::vector<double> p1, p2, h(2 * chunk);
+    std::vector<fo_cluster_pair> q;
+    cudaStream_t st = ctx->stream;
+    for (size_t c0 = 0; c0 < todo.size() && !s; c0 += chunk) {
+        const size_t nb = std::min(chunk, todo.size() - c0);
+        p1.resize(nb * per);
+        p2.resize(nb * per);
+        q.assign(nb, fo_cluster_pair{});
+        for (size_t k = 0; k < nb; ++k) {
+            memcpy(&p1[k * per], coordslist + (size_t)todo[c0 + k].first * per, per * sizeof(double));
+            memcpy(&p2[k * per], coordslist + (size_t)todo[c0 + k].second * per, per * sizeof(double));
+            q[k].natoms = natoms;
+            q[k].ngroups = (int)sizes.size();
+            q[k].jmax = l;
+            q[k].nrot = 1;
+            q[k].invert = 0;
+            q[k].sigma = kwidth;
+            q[k].coord_off = (int64_t)(k * natoms);
+        }
+        fo_plan *pl = nullptr;
+        s = fo_cluster_harm_plan_create(ctx, (int)nb, q.data(), p1.data(), p2.data(), perm.data(), sizes.data(), 1,
+                                        n, hwidth, &pl);
+        if (s) break;
+        cudaMemsetAsync(pl->d_coef, 0, pl->coef_bytes, st);
+        fo::launch_sph_center(pl->sb, st);
+        fo::launch_sph_ylm(pl->sb, pl->fp32, st);
+        fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
+        fo::launch_sph_coeff(pl->sb, pl->fp32, st);
+        fo::launch_isoft(pl->sb, pl->fp32, st);
+        fo::launch_pair_stats(pl->sb, pl->fp32, d_out, st);
+        cudaMemcpyAsync(h.data(), d_out, 2 * nb * sizeof(double), cudaMemcpyDeviceToHost, st);
+        s = cuda_check(ctx, cudaStreamSynchronize(st), "overlap matrices");
+        fo_plan_destroy(pl);
+        for (size_t k = 0; k < nb && !s; ++k) {
+            const int i1 = todo[c0 + k].first, i2 = todo[c0 + k].second;
+            norms[i1 + (size_t)nlist * i2] = norms[i2 + (size_t)nlist * i1] = h[2 * k];
+            maxovers[i1 + (size_t)nlist * i2] = maxovers[i2 + (size_t)nlist * i1] = h[2 * k + 1];
+        }
+    }
+    cudaFree(d_out);
+    return s;
 }
 
 fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz, double *kernelwidth,

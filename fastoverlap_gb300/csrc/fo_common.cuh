@@ -35,6 +35,9 @@ struct PairDev {
     long long lapstride; // LAP scratch bytes per candidate
     double sigma;
     double box[3];
+    int harm;         // cluster: 1 for the harmonic-oscillator basis (coordinates as given)
+    int harm_n;       // its largest order nmax
+    double harm_r0;   // its length scale (HWIDTH)
 };
 
 struct GroupDev {

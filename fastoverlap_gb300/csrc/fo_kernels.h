@@ -42,7 +42,11 @@ struct SphBuffers {
     void *grid;             // real T overlap grids
     const void *const *dtab;  // per bandwidth: Wigner table (T), layout [k][l][m1][m2]
     int npairs, ngroups, nslots, maxL, maxG, maxgroup;
+    int harm_n = -1;          // >= 0: harmonic-oscillator basis of this order (all pairs)
+    double *hd = nullptr;     // its radial overlaps d_nl, FP64 [side][slot][n][l <= maxL]
 };
+
+constexpr int kMaxHarmN = 40;   // largest harmonic order nmax
 
 // spherical stages
 void launch_sph_center(const SphBuffers &b, cudaStream_t s);
@@ -51,6 +55,7 @@ void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s);
 void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s);
 void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s);
 void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s);
+void launch_pair_stats(const SphBuffers &b, bool fp32, double *out, cudaStream_t s);
 void launch_wigner_table(int bw, double *d64, float *d32, cudaStream_t s);
 
 // periodic stages

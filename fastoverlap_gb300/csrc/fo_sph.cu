@@ -16,8 +16,9 @@
 namespace fo {
 
 // ---------------------------------------------------------------------------
-// Centre both structures and gather them into slot (group) order; choose the
-// Gaussian width when the caller passed sigma <= 0.  One block per pair.
+// Centre both structures (not for the harmonic basis) and gather them into
+// slot (group) order; choose the Gaussian width when the caller passed
+// sigma <= 0.  One block per pair.
 __global__ void k_sph_center(PairDev *pairs, const int *slot2orig, const double *pos1,
                              const double *pos2, double *xa, double *xb) {
     __shared__ double red[32 * 6];
@@ -50,11 +51,14 @@ __global__ void k_sph_center(PairDev *pairs, const int *slot2orig, const double 
         block_sum<double, 1>(acc, red);
         if (threadIdx.x == 0) pairs[p].sigma = acc[0] / (6.0 * n);
     }
+    // the harmonic basis (ALIGNHARM) takes the coordinates as given
+    double c[6];
+    for (int k = 0; k < 6; ++k) c[k] = P.harm ? 0.0 : s[k] / n;
     for (int sl = threadIdx.x; sl < n; sl += blockDim.x) {
         int o = slot2orig[base + sl];
         for (int k = 0; k < 3; ++k) {
-            xa[3 * (base + sl) + k] = pos2[3 * (base + o) + k] - s[k] / n;
-            xb[3 * (base + sl) + k] = pos1[3 * (base + o) + k] - s[3 + k] / n;
+            xa[3 * (base + sl) + k] = pos2[3 * (base + o) + k] - c[k];
+            xb[3 * (base + sl) + k] = pos1[3 * (base + o) + k] - c[3 + k];
         }
     }
 }
@@ -230,6 +234,69 @@ __global__ void k_sph_radial(const PairDev *pairs, const GroupDev *groups, const
     const T s0 = -expm1(T(-2) * x) / (T(2) * x);
     const T scale = pre * s0 / f;
     for (int l = 0; l <= L; ++l) out[l * lstride] = vals[l] * scale;
+}
+
+// ---------------------------------------------------------------------------
+// Harmonic-oscillator basis (SphericalHarmonicAlign): the radial weights of the
+// coefficient contraction are W_l(a, b) = sum_{n <= nmax} d_nl(r_a) d_nl(r_b),
+// d_nl(r) being the overlap of the Gaussian kernel at distance r with the basis
+// function of order (n, l) (HARMONICNL fastoverlap/f90/fastclusters.f90:492-540;
+// IMML = sum_n conj(c_B) c_A of DOTHARMONICCOEFFS :740-759 expanded over atom
+// pairs).  k_harm_dnl: d_nl of every slot of both structures in FP64 by the
+// recurrence in n from the closed form at n = 0, which runs to l = L + 2 nmax.
+// Output hd[((side * nslots + slot) * (nmax + 1) + n) * (maxL + 1) + l].
+constexpr int kHarmRow = kYlmMax + 2 * kMaxHarmN + 1;
+
+__global__ void k_harm_dnl(const PairDev *pairs, const int *slot2pair, const double *ra, const double *rb,
+                           double *hd, int nslots, int nmax, int maxL) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * nslots) return;
+    const int side = t / nslots, slot = t % nslots;
+    const PairDev &P = pairs[slot2pair[slot]];
+    const int L = P.L, lmax = L + 2 * nmax, w = maxL + 1;
+    const double rj = side ? rb[slot] : ra[slot], sigma = P.sigma, r0 = P.harm_r0;
+    double *out = hd + (size_t)t * (nmax + 1) * w;
+    double rows[3][kHarmRow];
+    double *pm2 = rows[0], *pm1 = rows[1], *cur = rows[2];
+    const double rs = 1.0 / (r0 * r0 + sigma * sigma), x = r0 * rs;
+    pm1[0] = sqrt(2.0 * sqrt(FO_PI) * (x * x * x)) * sigma * sigma * sigma * exp(-0.5 * rj * rj * rs) * 4 * FO_PI;
+    const double f = sqrt(2.0) * r0 * rj * rs;
+    for (int j = 1; j <= lmax; ++j) pm1[j] = f / sqrt(1.0 + 2.0 * j) * pm1[j - 1];
+    for (int l = 0; l <= L; ++l) out[l] = pm1[l];
+    const double q = sigma * sigma / rj / r0;
+    for (int i = 1; i <= nmax; ++i) {
+        const double si = sqrt((double)i), sm = sqrt(i - 1.0);
+        for (int j = 0; j <= lmax - 2 * i; ++j) {
+            double v = sqrt(i + j + 0.5) * pm1[j] - (2.0 * j + 3.0) * q * pm1[j + 1] - sqrt(i + j + 1.5) * pm1[j + 2];
+            cur[j] = (i == 1) ? v : (v + sm * pm2[j + 2]) / si;
+        }
+        for (int l = 0; l <= L; ++l) out[i * w + l] = cur[l];
+        double *tmp = pm2;
+        pm2 = pm1;
+        pm1 = cur;
+        cur = tmp;
+    }
+}
+
+// W_l(b, a) of every atom pair of every group, in the precision T of the
+// contraction (same layout as k_sph_radial).
+template <typename T>
+__global__ void k_harm_radial(const PairDev *pairs, const GroupDev *groups, const double *hd, T *W, int nslots,
+                              int nmax, int maxL) {
+    const GroupDev g = groups[blockIdx.y];
+    const int n = g.n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * n) return;
+    const int b = (int)(idx / n), a = (int)(idx % n), L = pairs[g.pair].L, w = maxL + 1;
+    const double *da = hd + (size_t)(g.slot0 + a) * (nmax + 1) * w;
+    const double *db = hd + (size_t)(nslots + g.slot0 + b) * (nmax + 1) * w;
+    T *out = W + g.w0 + (long long)b * n + a;
+    const long long lstride = (long long)n * n;
+    for (int l = 0; l <= L; ++l) {
+        double acc = 0;
+        for (int i = 0; i <= nmax; ++i) acc += da[i * w + l] * db[i * w + l];
+        out[l * lstride] = T(acc);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -471,6 +538,18 @@ void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s) {
 void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s) {
     long long nn = (long long)b.maxgroup * b.maxgroup;
     dim3 grid((unsigned)((nn + 255) / 256), (unsigned)b.ngroups);
+    if (b.harm_n >= 0) {
+        const int nth = 2 * b.nslots;
+        k_harm_dnl<<<(nth + 127) / 128, 128, 0, s>>>(b.pairs, b.slot2pair, b.ra, b.rb, b.hd, b.nslots, b.harm_n,
+                                                    b.maxL);
+        if (fp32)
+            k_harm_radial<float><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.hd, (float *)b.W, b.nslots, b.harm_n,
+                                                      b.maxL);
+        else
+            k_harm_radial<double><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.hd, (double *)b.W, b.nslots,
+                                                       b.harm_n, b.maxL);
+        return;
+    }
     if (fp32)
         k_sph_radial<float><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (float *)b.W, cutoff);
     else
@@ -492,6 +571,43 @@ void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s) {
                                                           (const double2 *)b.ylmB, (const double *)b.W,
                                                           (double2 *)b.coef);
     }
+}
+
+// CALCSIMILARITY's two numbers (fastoverlap/f90/fastclusters.f90:790-815) for
+// every pair of a plan: the squared norm of its SO(3) coefficients and the
+// maximum of its overlap grid (first orientation).  One block per pair;
+// out[2p] = norm, out[2p+1] = maximum.
+template <typename T, typename T2>
+__global__ void __launch_bounds__(256) k_pair_stats(const PairDev *pairs, const T2 *coef, const T *grid,
+                                                    double *out) {
+    __shared__ double red[32 * 2];
+    const PairDev &P = pairs[blockIdx.x];
+    const int W = 2 * P.L + 1;
+    const long long nc = (long long)(P.L + 1) * W * W, ng = (long long)P.G * P.G * P.G;
+    double v[1] = {0.0}, mx = -INFINITY;
+    for (long long i = threadIdx.x; i < nc; i += blockDim.x) {
+        const T2 c = coef[P.coef0 + i];
+        v[0] += (double)c.x * c.x + (double)c.y * c.y;
+    }
+    for (long long i = threadIdx.x; i < ng; i += blockDim.x) mx = fmax(mx, (double)grid[P.grid0 + i]);
+    block_sum<double, 1>(v, red);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[32 + (threadIdx.x >> 5)] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x + 31) / 32; ++w) mx = fmax(mx, red[32 + w]);
+        out[2 * blockIdx.x] = v[0];
+        out[2 * blockIdx.x + 1] = mx;
+    }
+}
+
+void launch_pair_stats(const SphBuffers &b, bool fp32, double *out, cudaStream_t s) {
+    if (fp32)
+        k_pair_stats<float, float2><<<b.npairs, 256, 0, s>>>(b.pairs, (const float2 *)b.coef,
+                                                            (const float *)b.grid, out);
+    else
+        k_pair_stats<double, double2><<<b.npairs, 256, 0, s>>>(b.pairs, (const double2 *)b.coef,
+                                                              (const double *)b.grid, out);
 }
 
 void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s) {

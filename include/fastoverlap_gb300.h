@@ -17,6 +17,11 @@
  *                             and ALIGN1 (:414-499) when nwave/nfspace are given
  *                             (f2py bulkfastoverlap.align, periodicAlignment.py:562-565)
  *   fo_bulk_calcdefaults   <- BULKFASTOVERLAP::CALCDEFAULTS fastoverlap/f90/fastbulk.f90:253-277
+ *   fo_cluster_align_harm  <- CLUSTERFASTOVERLAP::ALIGNHARM fastoverlap/f90/fastclusters.f90:271-391
+ *                             (f2py clusterfastoverlap.alignharm, sphericalAlignment.py:617)
+ *   fo_calc_overlap_matrices <- CLUSTERFASTOVERLAP::CALCOVERLAPMATRICES
+ *                             fastoverlap/f90/fastclusters.f90:846-866 (compareList, :622-663)
+ *   fo_cluster_harm_*      <- the same harmonic-basis alignment for many pairs
  *   fo_bulk_align_group    <- BULKFASTOVERLAP::ALIGNGROUP fastoverlap/f90/fastbulk.f90:336-412
  *                             (f2py bulkfastoverlap.aligngroup, periodicAlignment.py:570-605)
  *   fo_cluster_align_batch <- SphericalAlign.__call__ / SphericalAlignFortran.__call__
@@ -136,6 +141,17 @@ fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
                               const int *perm, const int *group_sizes, int index_base,
                               double *aligned, int *permbest, fo_pair_result *results);
 
+/* The cluster batch in the harmonic-oscillator basis (SphericalHarmonicAlign,
+ * ALIGNHARM): coefficients c_nlm of the coordinates as given (not centred),
+ * orders n <= nmax (<= 40) at length scale hwidth; every pair's sigma is the
+ * kernel width KWIDTH (> 0).  Outputs as fo_cluster_align_batch, aligned in
+ * pos1's own frame. */
+fo_status fo_cluster_harm_align_batch(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
+                                      const double *pos1, const double *pos2,
+                                      const int *perm, const int *group_sizes, int index_base,
+                                      int nmax, double hwidth, double *aligned, int *permbest,
+                                      fo_pair_result *results);
+
 /* ---- resident plans: upload once, run many times (inputs stay in HBM) ----
  * fo_plan_run launches the whole pipeline on the context's stream and
  * returns without synchronising; fo_plan_wait blocks until it is done.
@@ -153,6 +169,10 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
                               const double *pos1, const double *pos2,
                               const int *perm, const int *group_sizes, int index_base,
                               fo_plan **out);
+fo_status fo_cluster_harm_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs,
+                                      const double *pos1, const double *pos2,
+                                      const int *perm, const int *group_sizes, int index_base,
+                                      int nmax, double hwidth, fo_plan **out);
 fo_status fo_plan_run(fo_plan *plan);
 fo_status fo_plan_wait(fo_plan *plan);
 fo_status fo_plan_results(fo_plan *plan, double *aligned, int *permbest,
@@ -228,6 +248,28 @@ fo_status fo_get_bestperm(const fo_ctx *ctx, int *bestperm /* natoms, 1-based */
 fo_status fo_cluster_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms,
                            int debug, int l, double *kwidth, int nrotations, int perminvopt,
                            double *distance, double *dist2, double *rmatbest);
+
+/* CLUSTERFASTOVERLAP::ALIGNHARM (argument order of the Fortran routine, with
+ * PERMINVOPT last): the coordinates as given (coordsb is left as it is),
+ * harmonic-basis coefficients of order n at length scale hwidth, kernel
+ * width kwidth (> 0); coordsa becomes the aligned, permuted copy in
+ * coordsb's frame.  Every atom is refined in its own order and an inverted
+ * winner returns its own rotation, as CLUSTERFASTOVERLAP::ALIGN does (the
+ * Fortran ALIGNHARM keeps its per-group copies of the coordinates for the
+ * refinement and returns the non-inverted rotation; the results are the
+ * same for one permutation group in index order and non-inverted winners). */
+fo_status fo_cluster_align_harm(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms,
+                                int debug, int n, int l, double hwidth, double kwidth,
+                                double *distance, double *dist2, double *rmatbest,
+                                int nrotations, int perminvopt);
+
+/* CLUSTERFASTOVERLAP::CALCOVERLAPMATRICES: for every pair of structures of
+ * coordslist(3*natoms, nlist) (column-major), the squared norm of the
+ * harmonic-basis SO(3) coefficients (norms) and the maximum of the overlap
+ * grid (maxovers), both (nlist, nlist) and symmetric; groups of fo_setperm. */
+fo_status fo_calc_overlap_matrices(fo_ctx *ctx, const double *coordslist, int natoms, int nlist,
+                                   int n, int l, double hwidth, double kwidth,
+                                   double *norms, double *maxovers);
 
 /* BULKFASTOVERLAP::ALIGN (nwave = nfspace = 0) or ALIGN1 (both given). */
 fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natoms,
