@@ -44,7 +44,7 @@ class FoClusterPair(ctypes.Structure):
 
 class FoBulkPair(ctypes.Structure):
     _fields_ = [("natoms", ctypes.c_int), ("ngroups", ctypes.c_int), ("nwave", ctypes.c_int),
-                ("nfspace", ctypes.c_int), ("ndisps", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("nfspace", ctypes.c_int), ("ndisps", ctypes.c_int), ("ohcell", ctypes.c_int),
                 ("sigma", ctypes.c_double), ("box", ctypes.c_double * 3),
                 ("coord_off", ctypes.c_int64), ("perm_off", ctypes.c_int64),
                 ("group_off", ctypes.c_int64)]
@@ -112,6 +112,7 @@ EXPORTS = {
     "fo_plan_destroy": (None, [_vp]),
     "fo_setperm": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, ctypes.c_int]),
     "fo_get_bestperm": (ctypes.c_int, [_vp, _ip]),
+    "fo_set_ohcell": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fo_cluster_align": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         _dp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]),
     "fo_bulk_align": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,

@@ -189,7 +189,7 @@ class BulkBatch(_BatchBase):
     kind = "bulk"
 
     def __init__(self, ctx, pos1, pos2, boxes, perms=None, scale=0.0, nwave=0, nfspace=0,
-                 ndisps=10):
+                 ndisps=10, ohcell=False):
         super().__init__(ctx, pos1, pos2, perms)
         npairs = self.npairs
         boxes = np.broadcast_to(np.asarray(boxes, float).reshape(-1, 3), (npairs, 3))
@@ -197,6 +197,7 @@ class BulkBatch(_BatchBase):
         K = np.broadcast_to(np.asarray(nwave if nwave is not None else 0), (npairs,))
         M = np.broadcast_to(np.asarray(nfspace if nfspace is not None else 0), (npairs,))
         D = np.broadcast_to(np.asarray(ndisps), (npairs,))
+        O = np.broadcast_to(np.asarray(ohcell), (npairs,))
         desc = (_lib.FoBulkPair * npairs)()
         for k in range(npairs):
             dsc = desc[k]
@@ -205,6 +206,7 @@ class BulkBatch(_BatchBase):
             dsc.nwave = int(K[k])
             dsc.nfspace = int(M[k])
             dsc.ndisps = int(D[k])
+            dsc.ohcell = int(bool(O[k]))
             dsc.sigma = float(S[k])
             for c in range(3):
                 dsc.box[c] = float(boxes[k, c])

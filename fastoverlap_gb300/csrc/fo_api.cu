@@ -55,6 +55,7 @@ struct fo_ctx {
     std::vector<int> permgroup, npermsize;
     int perm_natoms = 0;
     std::vector<int> bestperm;
+    int ohcell = 0;   // COMMONS OHCELLT for fo_bulk_align
     double prof_ms[kNumKernels] = {0};
     int prof_n[kNumKernels] = {0};
     cudaEvent_t ev[64] = {};
@@ -691,6 +692,7 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
         double sg = q.sigma > 0 ? q.sigma : std::cbrt(q.box[0] * q.box[1] * q.box[2] / n) / 3.0;
         if (M < 2 * K + 1 || M > kMaxM) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: nfspace %d must lie in [2K+1, %d]", i, M, kMaxM); }
         if (nd > kMaxNrot) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: ndisps %d > %d", i, nd, kMaxNrot); }
+        if (q.ohcell) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: ohcell pairs run through fo_bulk_align_batch, not plans", i); }
         std::vector<int> s2o(n);
         fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
                                    index_base, s2o.data());
@@ -894,13 +896,78 @@ fo_status fo_cluster_align_batch(fo_ctx *ctx, int npairs, const fo_cluster_pair 
     return run_batch(ctx, pl, aligned, permbest, results);
 }
 
+// Operation op (0..47) of the cubic point group O_h as a signed permutation
+// of the axes, row-major: output axis r takes input axis P[op / 8][r] with
+// the sign of bit r of op % 8.  Operation 0 is the identity.
+static void oh_operation(int op, double M[9]) {
+    static const int P[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    for (int k = 0; k < 9; ++k) M[k] = 0.0;
+    for (int r = 0; r < 3; ++r) M[3 * r + P[op / 8][r]] = ((op % 8) >> r & 1) ? -1.0 : 1.0;
+}
+
 fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs, const double *pos1,
                               const double *pos2, const int *perm, const int *group_sizes,
                               int index_base, double *aligned, int *permbest, fo_pair_result *results) {
-    fo_plan *pl = nullptr;
-    fo_status s = fo_bulk_plan_create(ctx, npairs, pairs, pos1, pos2, perm, group_sizes, index_base, &pl);
+    bool oh = false;
+    for (int i = 0; pairs && i < npairs; ++i) oh = oh || pairs[i].ohcell;
+    if (!oh) {
+        fo_plan *pl = nullptr;
+        fo_status s = fo_bulk_plan_create(ctx, npairs, pairs, pos1, pos2, perm, group_sizes, index_base, &pl);
+        if (s) return s;
+        return run_batch(ctx, pl, aligned, permbest, results);
+    }
+    // OHCELLT (ALIGN1, fastbulk.f90:458-481): every operation of an ohcell pair
+    // is a pair of its own, pos2 transformed; the best of the 48 is kept
+    if (!ctx || !pos1 || !pos2 || !results) return set_err(ctx, FO_ERR_BAD_ARGS, "null argument");
+    std::vector<fo_bulk_pair> q;
+    std::vector<int> first(npairs);
+    size_t natoms = 0;
+    for (int i = 0; i < npairs; ++i) {
+        first[i] = (int)q.size();
+        for (int op = 0; op < (pairs[i].ohcell ? 48 : 1); ++op) {
+            fo_bulk_pair e = pairs[i];
+            e.ohcell = 0;
+            e.coord_off = (int64_t)natoms;
+            natoms += (size_t)std::max(0, e.natoms);
+            q.push_back(e);
+        }
+    }
+    std::vector<double> p1(3 * natoms), p2(3 * natoms), al(aligned ? 3 * natoms : 0);
+    std::vector<int> pb(permbest ? natoms : 0);
+    std::vector<fo_pair_result> res(q.size());
+    for (int i = 0; i < npairs; ++i) {
+        const size_t n = (size_t)std::max(0, pairs[i].natoms);
+        const double *a1 = pos1 + 3 * pairs[i].coord_off, *a2 = pos2 + 3 * pairs[i].coord_off;
+        for (int k = first[i]; k < (i + 1 < npairs ? first[i + 1] : (int)q.size()); ++k) {
+            double M[9];
+            oh_operation(k - first[i], M);
+            double *b1 = &p1[3 * q[k].coord_off], *b2 = &p2[3 * q[k].coord_off];
+            memcpy(b1, a1, 3 * n * sizeof(double));
+            for (size_t j = 0; j < n; ++j)
+                for (int r = 0; r < 3; ++r)
+                    b2[3 * j + r] = M[3 * r] * a2[3 * j] + M[3 * r + 1] * a2[3 * j + 1] + M[3 * r + 2] * a2[3 * j + 2];
+        }
+    }
+    fo_status s = fo_bulk_align_batch(ctx, (int)q.size(), q.data(), p1.data(), p2.data(), perm, group_sizes,
+                                      index_base, aligned ? al.data() : nullptr, permbest ? pb.data() : nullptr,
+                                      res.data());
     if (s) return s;
-    return run_batch(ctx, pl, aligned, permbest, results);
+    for (int i = 0; i < npairs; ++i) {
+        const int k0 = first[i], k1 = (i + 1 < npairs) ? first[i + 1] : (int)q.size();
+        int best = k0, ncand = 0;
+        for (int k = k0; k < k1; ++k) {
+            ncand += res[k].ncand;
+            const bool ok = res[k].status == 0, bok = res[best].status == 0;
+            if ((ok && !bok) || (ok && bok && res[k].dist < res[best].dist)) best = k;
+        }
+        results[i] = res[best];
+        results[i].ncand = ncand;
+        if (pairs[i].ohcell) oh_operation(best - k0, results[i].rmat);
+        const size_t n = (size_t)std::max(0, pairs[i].natoms);
+        if (aligned) memcpy(aligned + 3 * pairs[i].coord_off, &al[3 * q[best].coord_off], 3 * n * sizeof(double));
+        if (permbest) memcpy(permbest + pairs[i].coord_off, &pb[q[best].coord_off], n * sizeof(int));
+    }
+    return FO_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1028,6 +1095,12 @@ fo_status fo_setperm(fo_ctx *ctx, int natoms, const int *permgroup, const int *n
     return FO_OK;
 }
 
+fo_status fo_set_ohcell(fo_ctx *ctx, int ohcell) {
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    ctx->ohcell = ohcell ? 1 : 0;
+    return FO_OK;
+}
+
 fo_status fo_get_bestperm(const fo_ctx *ctx, int *bestperm) {
     if (!ctx || !bestperm || ctx->bestperm.empty()) return FO_ERR_BAD_ARGS;
     memcpy(bestperm, ctx->bestperm.data(), ctx->bestperm.size() * sizeof(int));
@@ -1095,6 +1168,7 @@ fo_status fo_bulk_align(fo_ctx *ctx, double *coordsb, double *coordsa, int natom
     q.nwave = nwave;
     q.nfspace = nfspace;
     q.ndisps = ndisplacements;
+    q.ohcell = ctx->ohcell;
     q.sigma = kwidth;
     q.box[0] = boxlx;
     q.box[1] = boxly;

@@ -142,8 +142,9 @@ class PeriodicAlignFortran(object):
             self.perm = [self.permgroup - 1]
 
     def align(self, pos1, pos2, ndisps=10, perm=None, ohcell=False, debug=False):
-        if ohcell:
-            raise NotImplementedError("the 48 octahedral-cell operations (OHCELL) are not built")
+        """With ohcell, pos2 is also tried under the 48 operations of the cubic
+        point group (COMMONS OHCELLT); X2 is then the transformed, aligned pos2
+        and self.ohop the winning operation (row-major 3x3)."""
         pos1 = np.asarray(pos1, float).reshape(-1, 3)
         pos2 = np.asarray(pos2, float).reshape(-1, 3)
         if perm is not None:
@@ -151,11 +152,13 @@ class PeriodicAlignFortran(object):
         if len(pos2) != self.Natoms:
             self.setPerm([np.arange(len(pos2))])
         b = BulkBatch(self.ctx, [pos1], [pos2], self.boxvec, [self.perm],
-                      scale=self.scale if self.scale else 0.0, nwave=0, nfspace=0, ndisps=ndisps)
+                      scale=self.scale if self.scale else 0.0, nwave=0, nfspace=0, ndisps=ndisps,
+                      ohcell=bool(ohcell))
         out = b.run()
         r = out["result"][0]
         if r["status"] != 0:
             raise _lib.FoError(int(r["status"]), "periodic alignment failed")
+        self.ohop = np.asarray(r["rmat"], float).reshape(3, 3).copy()
         return float(r["dist"]), pos1.copy(), out["aligned"][0].copy(), out["perm"][0].copy()
 
     def alignGroup(self, coords, ndisps=1):

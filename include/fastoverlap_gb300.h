@@ -94,7 +94,7 @@ typedef struct {
     int     nwave;       /* K: (2K+1)^3 wave vectors; <= 0 -> ceil(1.3 N^1/3) */
     int     nfspace;     /* M: M^3 translation grid; <= 0 -> FASTLEN(4K+3)    */
     int     ndisps;      /* candidate displacements; <= 0 -> 10               */
-    int     reserved;
+    int     ohcell;      /* 1: also the 48 cubic-cell operations (OHCELLT)    */
     double  sigma;       /* <= 0 -> (V/N)^(1/3)/3                             */
     double  box[3];      /* orthorhombic box lengths                          */
     int64_t coord_off;
@@ -136,6 +136,13 @@ fo_status fo_cluster_align_batch(fo_ctx *ctx, int npairs, const fo_cluster_pair 
                                  const int *perm, const int *group_sizes, int index_base,
                                  double *aligned, int *permbest, fo_pair_result *results);
 
+/* A pair with ohcell = 1 is aligned for each of the 48 operations of the
+ * cubic point group applied to pos2 (signed permutations of x, y, z; ALIGN1
+ * with OHCELLT, fastoverlap/f90/fastbulk.f90:458-481) and the smallest
+ * distance wins (the first operation on ties, the identity first).  Its
+ * result's rmat is that operation (row-major; aligned = op(pos2)[perm] +
+ * disp), its ncand counts all 48 searches.  Resident plans take no ohcell
+ * pairs. */
 fo_status fo_bulk_align_batch(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs,
                               const double *pos1, const double *pos2,
                               const int *perm, const int *group_sizes, int index_base,
@@ -241,6 +248,8 @@ size_t    fo_bulk_overlap_noalloc_scratch_bytes(void);
 fo_status fo_setperm(fo_ctx *ctx, int natoms, const int *permgroup, const int *npermsize,
                      int npermgroup);
 fo_status fo_get_bestperm(const fo_ctx *ctx, int *bestperm /* natoms, 1-based */);
+/* COMMONS OHCELLT for fo_bulk_align: 1 searches the 48 cubic operations. */
+fo_status fo_set_ohcell(fo_ctx *ctx, int ohcell);
 
 /* CLUSTERFASTOVERLAP::ALIGN: coordsb is centred in place, coordsa becomes the
  * aligned, permuted copy; kwidth <= 0 is replaced by the chosen width;

@@ -300,6 +300,32 @@ def bulk_align(pos1, pos2, box, perm=None, sigma=0.0, nwave=0, nfspace=0, ndisps
                 ncand=r.ncand, sigma=r.sigma, overlap_max=r.overlap_max)
 
 
+def oh_operation(op):
+    """Operation op (0..47) of the cubic point group as a signed axis
+    permutation (row-major): output axis r takes input axis P[op // 8][r],
+    negated when bit r of op % 8 is set.  Operation 0 is the identity."""
+    P = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    M = np.zeros((3, 3))
+    for r in range(3):
+        M[r, P[op // 8][r]] = -1.0 if (op % 8) >> r & 1 else 1.0
+    return M
+
+
+def bulk_align_ohcell(pos1, pos2, box, perm=None, sigma=0.0, nwave=0, nfspace=0, ndisps=10):
+    """ALIGN1 with OHCELLT (fastbulk.f90:458-481): the alignment of pos1 with
+    op(pos2) for the 48 cubic operations, the smallest distance kept (the
+    first operation on ties).  The overlap of each operation is formed from
+    the transformed structure.  Returns the best dict with 'op' and 'M'."""
+    p2 = np.asarray(pos2, dtype=np.float64).reshape(-1, 3)
+    best = None
+    for op in range(48):
+        M = oh_operation(op)
+        r = bulk_align(pos1, p2 @ M.T, box, perm, sigma, nwave, nfspace, ndisps)
+        if r["status"] == 0 and (best is None or r["dist"] < best["dist"]):
+            best = dict(r, op=op, M=M)
+    return best
+
+
 def cluster_align_many(pairs, nrot=10, invert=True, cutoff=True, nthreads=None):
     """pairs: list of dicts(pos1, pos2, perm, Jmax, sigma). Returns distances."""
     nthreads = nthreads or os.cpu_count() or 1
