@@ -527,6 +527,21 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     return FO_OK;
 }
 
+// True when pair i's atoms start where pair i-1's end (the packed order the
+// plans use), so the caller's coordinate arrays can be uploaded as they are
+// and results downloaded straight into the caller's arrays.
+extern "C++" {
+template <typename PairT>
+static bool packed_in_order(const PairT *pairs, int npairs) {
+    long long off = 0;
+    for (int i = 0; i < npairs; ++i) {
+        if (pairs[i].coord_off != off || pairs[i].natoms < 0) return false;
+        off += pairs[i].natoms;
+    }
+    return true;
+}
+}
+
 // harm_n < 0: the Gaussian-kernel coefficients of ALIGN; harm_n >= 0: the
 // harmonic-oscillator basis of ALIGNHARM (order harm_n, length scale harm_r0).
 static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_pair *pairs, const double *pos1,
@@ -552,6 +567,7 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
     std::vector<int> cand_list;
     long long ylm_n = 0, w_n = 0, coef_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
     int atom0 = 0, cand0 = 0;
+    const bool contig = packed_in_order(pairs, npairs);   // upload straight from the caller's arrays
     for (int i = 0; i < npairs; ++i) {
         const fo_cluster_pair &q = pairs[i];
         const int n = q.natoms, L = q.jmax;
@@ -617,8 +633,10 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
             slot2pair.push_back(i);
         }
         for (int c = 0; c < P.norient * P.nrot; ++c) cand2pair.push_back(i);
-        hpos1.insert(hpos1.end(), pos1 + 3 * q.coord_off, pos1 + 3 * (q.coord_off + n));
-        hpos2.insert(hpos2.end(), pos2 + 3 * q.coord_off, pos2 + 3 * (q.coord_off + n));
+        if (!contig) {
+            hpos1.insert(hpos1.end(), pos1 + 3 * q.coord_off, pos1 + 3 * (q.coord_off + n));
+            hpos2.insert(hpos2.end(), pos2 + 3 * q.coord_off, pos2 + 3 * (q.coord_off + n));
+        }
         ylm_n += (long long)n * (L + 1) * (L + 1);
         coef_n += (long long)(L + 1) * (2 * L + 1) * (2 * L + 1);
         grid_n += (long long)P.norient * P.G * P.G * P.G;
@@ -640,8 +658,8 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
     build_buckets(pl, rassign, cand_list);
     pl->harm_n = harm_n >= 0 ? harm_n : -1;
     pl->harm_d = harm_n >= 0 ? 2 * (size_t)pl->nslots * (harm_n + 1) * (pl->maxL + 1) : 0;
-    s = plan_common_alloc(ctx, pl, hpos1.data(), hpos2.data(), slot2orig, slot2pair, cand2pair,
-                          cand_list, ylm_n, w_n, coef_n, grid_n, 0, lap_total);
+    s = plan_common_alloc(ctx, pl, contig ? pos1 : hpos1.data(), contig ? pos2 : hpos2.data(), slot2orig,
+                          slot2pair, cand2pair, cand_list, ylm_n, w_n, coef_n, grid_n, 0, lap_total);
     if (s) { fo_plan_destroy(pl); return s; }
     pl->sb.dtab = pl->fp32 ? (const void *const *)ctx->d_dtab32 : (const void *const *)ctx->d_dtab64;
     *out = pl;
@@ -680,6 +698,7 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
     std::vector<int> cand_list;
     long long fgrid_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
     int atom0 = 0, cand0 = 0;
+    const bool contig = packed_in_order(pairs, npairs);   // upload straight from the caller's arrays
     for (int i = 0; i < npairs; ++i) {
         const fo_bulk_pair &q = pairs[i];
         const int n = q.natoms;
@@ -744,8 +763,10 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
             slot2pair.push_back(i);
         }
         for (int c = 0; c < P.nrot; ++c) cand2pair.push_back(i);
-        hpos1.insert(hpos1.end(), pos1 + 3 * q.coord_off, pos1 + 3 * (q.coord_off + n));
-        hpos2.insert(hpos2.end(), pos2 + 3 * q.coord_off, pos2 + 3 * (q.coord_off + n));
+        if (!contig) {
+            hpos1.insert(hpos1.end(), pos1 + 3 * q.coord_off, pos1 + 3 * (q.coord_off + n));
+            hpos2.insert(hpos2.end(), pos2 + 3 * q.coord_off, pos2 + 3 * (q.coord_off + n));
+        }
         fgrid_n += (long long)M * M * M;
         grid_n += (long long)M * M * M;
         candatom += (long long)P.nrot * n;
@@ -759,8 +780,9 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
     pl->ncand = cand0;
     pl->ngroups = (int)pl->hg.size();
     build_buckets(pl, rassign, cand_list);
-    fo_status s = plan_common_alloc(ctx, pl, hpos1.data(), hpos2.data(), slot2orig, slot2pair,
-                                    cand2pair, cand_list, 0, 0, 0, grid_n, fgrid_n, lap_total);
+    fo_status s = plan_common_alloc(ctx, pl, contig ? pos1 : hpos1.data(), contig ? pos2 : hpos2.data(),
+                                    slot2orig, slot2pair, cand2pair, cand_list, 0, 0, 0, grid_n, fgrid_n,
+                                    lap_total);
     if (s) { fo_plan_destroy(pl); return s; }
     *out = pl;
     return FO_OK;
@@ -823,9 +845,24 @@ fo_status fo_plan_results(fo_plan *pl, double *aligned, int *permbest, fo_pair_r
     fo_ctx *ctx = pl->ctx;
     const int np = pl->npairs, ns = pl->nslots;
     std::vector<fo_pair_result> res(np);
+    cudaStream_t st = ctx->stream;
+    // pairs packed in slot order: the per-atom outputs go straight to the caller
+    bool direct = true;
+    for (int i = 0; i < np && direct; ++i) direct = pl->caller_off[i] == pl->hp[i].atom0;
+    if (direct) {
+        cudaMemcpyAsync(res.data(), pl->rb.results, np * sizeof(fo_pair_result), cudaMemcpyDeviceToHost, st);
+        if (aligned)
+            cudaMemcpyAsync(aligned, pl->rb.aligned, 3 * (size_t)ns * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (permbest) cudaMemcpyAsync(permbest, pl->rb.permbest, (size_t)ns * sizeof(int), cudaMemcpyDeviceToHost, st);
+        fo_status s = cuda_check(ctx, cudaStreamSynchronize(st), "result download");
+        if (s) return s;
+        if (permbest && pl->index_base)
+            for (int j = 0; j < ns; ++j) permbest[j] += pl->index_base;
+        if (results) memcpy(results, res.data(), np * sizeof(fo_pair_result));
+        return FO_OK;
+    }
     std::vector<double> al(aligned ? 3 * (size_t)ns : 0);
     std::vector<int> pb(permbest ? ns : 0);
-    cudaStream_t st = ctx->stream;
     cudaMemcpyAsync(res.data(), pl->rb.results, np * sizeof(fo_pair_result), cudaMemcpyDeviceToHost, st);
     if (aligned) cudaMemcpyAsync(al.data(), pl->rb.aligned, al.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (permbest) cudaMemcpyAsync(pb.data(), pl->rb.permbest, pb.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
