@@ -139,8 +139,10 @@ class _BatchBase(object):
         out = {"result": res, "dist": res["dist"].copy(), "status": res["status"].copy()}
         if aligned is not None:
             al = aligned.reshape(-1, 3)
-            out["aligned"] = [al[o:o + n] for o, n in zip(self.pk.off, self.pk.n)]
-            out["perm"] = [permbest[o:o + n] for o, n in zip(self.pk.off, self.pk.n)]
+            if not hasattr(self, "_spans"):   # Python ints slice faster than numpy scalars
+                self._spans = list(zip(self.pk.off.tolist(), (self.pk.off + self.pk.n).tolist()))
+            out["aligned"] = [al[a:b] for a, b in self._spans]
+            out["perm"] = [permbest[a:b] for a, b in self._spans]
         return out
 
 

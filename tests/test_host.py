@@ -150,3 +150,23 @@ def test_clock_sampler_parses_reasons():
                 "0, 1990, 2070, 910.0, 0x0, Not Active, Not Active, Not Active, Not Active"]
     r = cs.stop()
     assert r["sm_mhz"] == 1985 and r["sm_max_mhz"] == 2070 and r["reasons"] == ["sw_power_cap"]
+
+
+def test_batch_result_unpacking_spans():
+    """Per-pair views of the packed outputs (no GPU: the unpacking is host code)."""
+    import numpy as np
+    from fastoverlap_gb300 import batch, _lib
+
+    class Pk(object):
+        pass
+
+    b = batch.ClusterBatch.__new__(batch.ClusterBatch)
+    b.pk = Pk()
+    b.pk.n = np.array([3, 5, 2])
+    b.pk.off = np.array([0, 3, 8])
+    b.pk.natoms_total = 10
+    res = np.zeros(3, _lib.RESULT_DTYPE)
+    out = b._unpack(res, np.arange(30.0), np.arange(10, dtype=np.int32))
+    assert [x.shape for x in out["aligned"]] == [(3, 3), (5, 3), (2, 3)]
+    assert [x.tolist() for x in out["perm"]] == [[0, 1, 2], [3, 4, 5, 6, 7], [8, 9]]
+    assert out["aligned"][1][0].tolist() == [9.0, 10.0, 11.0]
