@@ -4,9 +4,12 @@
 // (bulk) the moved structure by the candidate, then alternate
 //   per-group squared distances (60 nearest per row when a group has more
 //   than 60 atoms) -> integer costs INT(d^2 * 1e6) -> sparse Jonker-Volgenant
-//   assignment -> Kearsley rotation (cluster) or mean minimum-image
+//   assignment -> best rotation (cluster) or mean minimum-image
 //   displacement (bulk)
-// until no atom changes partner, the distance grows, or 21 tries.
+// until no atom changes partner, the distance grows, or 21 tries.  The FP64
+// form takes the rotation from the Kearsley matrix as FINDROTATION does; the
+// mixed form from Horn's matrix of the 3x3 correlation (the same minimiser),
+// with its FP64 work spread one matrix entry per lane.
 // Candidates are launched in buckets of equal shared-memory footprint so
 // small problems pack many warps per SM; the assignment arrays live in
 // shared memory when they fit and in per-candidate global scratch otherwise.
