@@ -102,6 +102,7 @@ EXPORTS = {
                                            ctypes.c_int, _dp, _ip, _vp]),
     "fo_cluster_plan_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
                                               ctypes.c_int, ctypes.POINTER(_vp)]),
+    "fo_plan_set_graph": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fo_bulk_plan_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
                                            ctypes.c_int, ctypes.POINTER(_vp)]),
     "fo_plan_run": (ctypes.c_int, [_vp]),

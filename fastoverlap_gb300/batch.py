@@ -100,6 +100,11 @@ class _BatchBase(object):
         _lib.track("plans", self)
         return self
 
+    def plan_graph(self, on=True):
+        """Replay the plan's runs as a captured CUDA graph (from the second run on)."""
+        self.ctx.check(self.ctx.lib.fo_plan_set_graph(self.plan_h, int(bool(on))), "plan graph")
+        return self
+
     def plan_run(self):
         self.ctx.check(self.ctx.lib.fo_plan_run(self.plan_h), "plan run")
 

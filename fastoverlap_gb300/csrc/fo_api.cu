@@ -76,6 +76,9 @@ struct fo_plan {
     int npairs = 0, nslots = 0, ncand = 0, ngroups = 0;
     int maxL = 0, maxG = 0, maxgroup = 0, maxn = 0;
     int index_base = 0;
+    bool use_graph = false;  // runs after the first replay a captured CUDA graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
     int harm_n = -1;         // >= 0: harmonic-oscillator basis of this order
     size_t harm_d = 0;       // doubles of its radial overlap buffer
     std::vector<fo::PairDev> hp;
@@ -788,14 +791,15 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
     return FO_OK;
 }
 
-fo_status fo_plan_run(fo_plan *pl) {
-    if (!pl) return FO_ERR_BAD_ARGS;
+// The plan's launch sequence on the context's stream (the refinement buckets
+// fork onto the auxiliary streams and join back).  events: per-stage profile
+// events (not while a graph is captured).
+static void plan_enqueue(fo_plan *pl, bool events) {
     fo_ctx *ctx = pl->ctx;
-    cudaSetDevice(ctx->opts.device);
     cudaStream_t st = ctx->stream;
-    for (auto e : pl->evs) cudaEventDestroy(e);
-    pl->evs.clear();
-    pl->ev_kid.clear();
+    auto rec_event = [&](fo_plan *p, int kid) {
+        if (events) ::rec_event(p, kid);
+    };
     rec_event(pl, -1);
     cudaMemsetAsync(pl->d_pstatus, 0, pl->npairs * sizeof(int), st);
     cudaMemsetAsync(pl->d_npeaks, 0, 2 * pl->npairs * sizeof(int), st);
@@ -818,7 +822,45 @@ fo_status fo_plan_run(fo_plan *pl) {
     fo::launch_refine(pl->rb, st, ctx->aux, fo_ctx::kAux, ctx->fork, ctx->join);
     rec_event(pl, K_REFINE);
     fo::launch_select(pl->rb, st);              rec_event(pl, K_SELECT);
-    return cuda_check(ctx, cudaGetLastError(), "kernel launch");
+}
+
+fo_status fo_plan_run(fo_plan *pl) {
+    if (!pl) return FO_ERR_BAD_ARGS;
+    fo_ctx *ctx = pl->ctx;
+    cudaSetDevice(ctx->opts.device);
+    cudaStream_t st = ctx->stream;
+    if (pl->use_graph && pl->gexec) return cuda_check(ctx, cudaGraphLaunch(pl->gexec, st), "graph launch");
+    for (auto e : pl->evs) cudaEventDestroy(e);
+    pl->evs.clear();
+    pl->ev_kid.clear();
+    plan_enqueue(pl, !pl->use_graph);
+    fo_status s = cuda_check(ctx, cudaGetLastError(), "kernel launch");
+    if (s || !pl->use_graph) return s;
+    // this run went eagerly (kernel attributes are set once, outside any
+    // capture); the same sequence is captured for the runs that follow
+    s = cuda_check(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (s) return s;
+    plan_enqueue(pl, false);
+    cudaGraph_t g = nullptr;
+    s = cuda_check(ctx, cudaStreamEndCapture(st, &g), "end capture");
+    if (s) return s;
+    pl->graph = g;
+    return cuda_check(ctx, cudaGraphInstantiate(&pl->gexec, g, 0), "graph instantiate");
+}
+
+static void drop_graph(fo_plan *pl) {
+    if (pl->gexec) cudaGraphExecDestroy(pl->gexec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    pl->gexec = nullptr;
+    pl->graph = nullptr;
+}
+
+fo_status fo_plan_set_graph(fo_plan *pl, int on) {
+    if (!pl) return FO_ERR_BAD_ARGS;
+    cudaSetDevice(pl->ctx->opts.device);
+    if (!on) drop_graph(pl);
+    pl->use_graph = on != 0;
+    return FO_OK;
 }
 
 fo_status fo_plan_wait(fo_plan *pl) {
@@ -898,6 +940,7 @@ void fo_plan_destroy(fo_plan *pl) {
     if (!pl) return;
     cudaSetDevice(pl->ctx->opts.device);
     cudaStreamSynchronize(pl->ctx->stream);
+    drop_graph(pl);
     for (auto e : pl->evs) cudaEventDestroy(e);
     fo_ctx *ctx = pl->ctx;
     if (pl->dmem) {

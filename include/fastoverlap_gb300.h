@@ -181,6 +181,11 @@ fo_status fo_cluster_harm_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_
                                       const int *perm, const int *group_sizes, int index_base,
                                       int nmax, double hwidth, fo_plan **out);
 fo_status fo_plan_run(fo_plan *plan);
+/* on = 1: the next fo_plan_run runs eagerly and captures its launch sequence
+ * (all streams) as a CUDA graph; later runs replay the graph with one launch.
+ * Per-stage profile times are not recorded while graphs are used.  on = 0
+ * drops the graph. */
+fo_status fo_plan_set_graph(fo_plan *plan, int on);
 fo_status fo_plan_wait(fo_plan *plan);
 fo_status fo_plan_results(fo_plan *plan, double *aligned, int *permbest,
                           fo_pair_result *results);

@@ -160,3 +160,31 @@ def test_large_bandwidth_properties(fo, prec, n):
     assert sorted(r["perm"][na:]) == list(range(na, n))
     assert abs(np.linalg.norm(r["X1"] - r["X2"]) - r["dist"]) < 1e-8
     assert r["dist"] < 0.05 * np.sqrt(3 * n) * 1.5   # noise level of the generator
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_plan_graph_replay_equals_eager(fo, prec):
+    """A plan replayed as a captured CUDA graph gives the eager results, bit for bit."""
+    ps = synth.config2(24)
+    ctx = fo.Context(precision=prec)
+    mk = lambda: fo.ClusterBatch(ctx, [p["pos1"] for p in ps], [p["pos2"] for p in ps],
+                                 [p["perm"] for p in ps], Jmax=[p["Jmax"] for p in ps], scale=0.3,
+                                 nrot=10).plan()
+    eager = mk()
+    eager.plan_run()
+    eager.plan_wait()
+    ref = eager.plan_results(True)
+    eager.close()
+    g = mk().plan_graph()
+    for _ in range(3):   # eager + capture, then two replays
+        g.plan_run()
+        g.plan_wait()
+        out = g.plan_results(True)
+        np.testing.assert_array_equal(out["dist"], ref["dist"])
+        for a, b in zip(out["aligned"], ref["aligned"]):
+            np.testing.assert_array_equal(a, b)
+    g.plan_graph(False)
+    g.plan_run()
+    g.plan_wait()
+    np.testing.assert_array_equal(g.plan_results(False)["dist"], ref["dist"])
+    g.close()
