@@ -1352,6 +1352,266 @@ void orc_calc_similarity(const double *c1, const double *c2, int ngroups, int nm
 }
 
 /* ------------------------------------------------------------------------ */
+/* Branch and bound over rotations (the upstream Python BranchandBoundMaster
+ * with BranchNodeCluster, fastoverlap/bnbAlignment.py:23-104,204-277): nodes
+ * are cubes of angle-axis vectors; a node's lower bound is the assignment
+ * over the smallest squared distances any rotation in the cube can reach
+ * (angular bound on the atom-pair angle), its upper bound the assignment
+ * distance at the cube's centre.  Best-first by lower bound until the lower
+ * bound is within rtol * best + atol of the best upper bound.              */
+
+/* Dense linear assignment on double costs (shortest augmenting paths with
+ * row and column potentials, Jonker & Volgenant 1987): col[i] = column of
+ * row i; returns the optimal cost.                                          */
+static double orc_lap_dense(int n, const double *c, int *col) {
+    double *u = calloc(n + 1, sizeof(double)), *v = calloc(n + 1, sizeof(double));
+    double *minv = malloc(sizeof(double) * (n + 1));
+    int *p = calloc(n + 1, sizeof(int)), *way = calloc(n + 1, sizeof(int));
+    char *used = malloc(n + 1);
+    for (int i = 1; i <= n; ++i) {   /* 1-based, column 0 is the virtual start */
+        p[0] = i;
+        int j0 = 0;
+        for (int j = 0; j <= n; ++j) { minv[j] = HUGE_VAL; used[j] = 0; }
+        do {
+            used[j0] = 1;
+            const int i0 = p[j0];
+            double delta = HUGE_VAL;
+            int j1 = 0;
+            for (int j = 1; j <= n; ++j)
+                if (!used[j]) {
+                    const double cur = c[(size_t)(i0 - 1) * n + (j - 1)] - u[i0] - v[j];
+                    if (cur < minv[j]) { minv[j] = cur; way[j] = j0; }
+                    if (minv[j] < delta) { delta = minv[j]; j1 = j; }
+                }
+            for (int j = 0; j <= n; ++j)
+                if (used[j]) { u[p[j]] += delta; v[j] -= delta; }
+                else minv[j] -= delta;
+            j0 = j1;
+        } while (p[j0] != 0);
+        do {
+            const int j1 = way[j0];
+            p[j0] = p[j1];
+            j0 = j1;
+        } while (j0);
+    }
+    double tot = 0;
+    for (int j = 1; j <= n; ++j) {
+        col[p[j] - 1] = j - 1;
+        tot += c[(size_t)(p[j] - 1) * n + (j - 1)];
+    }
+    free(u); free(v); free(minv); free(p); free(way); free(used);
+    return tot;
+}
+
+/* angle-axis vector -> rotation matrix (row-major), Rodrigues' formula    */
+static void orc_angle_axis(const double w[3], double M[9]) {
+    const double th = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    if (th == 0.0) {
+        for (int k = 0; k < 9; ++k) M[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        return;
+    }
+    const double x = w[0] / th, y = w[1] / th, z = w[2] / th, c = cos(th), s = sin(th), C = 1 - c;
+    const double xs = x * s, ys = y * s, zs = z * s, xC = x * C, yC = y * C, zC = z * C;
+    const double xyC = x * yC, yzC = y * zC, zxC = z * xC;
+    M[0] = x * xC + c; M[1] = xyC - zs;    M[2] = zxC + ys;
+    M[3] = xyC + zs;   M[4] = y * yC + c;  M[5] = yzC - xs;
+    M[6] = zxC - ys;   M[7] = yzC + xs;    M[8] = z * zC + c;
+}
+
+typedef struct {
+    double rot[3], width, lower, upper;
+    int sign;        /* +1: pos2, -1: the inverted pos2 */
+    int id;
+} orc_bnb_node;
+
+/* binary min-heap on (lower) with the sift rules of Python's heapq: a push
+ * sifts the new item up past strictly larger parents; a pop moves the last
+ * item to the root, walks it down to a leaf along the smaller child (the
+ * right one only when strictly smaller) and then sifts it up.            */
+typedef struct { orc_bnb_node *a; int n, cap; } orc_heap;
+static void heap_up(orc_heap *h, int start, int pos) {
+    orc_bnb_node it = h->a[pos];
+    while (pos > start) {
+        const int par = (pos - 1) >> 1;
+        if (it.lower < h->a[par].lower) { h->a[pos] = h->a[par]; pos = par; }
+        else break;
+    }
+    h->a[pos] = it;
+}
+static void heap_push(orc_heap *h, orc_bnb_node x) {
+    if (h->n == h->cap) { h->cap = h->cap ? 2 * h->cap : 64; h->a = realloc(h->a, sizeof(orc_bnb_node) * h->cap); }
+    h->a[h->n++] = x;
+    heap_up(h, 0, h->n - 1);
+}
+static orc_bnb_node heap_pop(orc_heap *h) {
+    orc_bnb_node last = h->a[--h->n];
+    if (h->n == 0) return last;
+    orc_bnb_node top = h->a[0];
+    h->a[0] = last;
+    int pos = 0;
+    const int end = h->n;
+    orc_bnb_node it = h->a[0];
+    int child = 1;
+    while (child < end) {
+        const int right = child + 1;
+        if (right < end && !(h->a[child].lower < h->a[right].lower)) child = right;
+        h->a[pos] = h->a[child];
+        pos = child;
+        child = 2 * pos + 1;
+    }
+    h->a[pos] = it;
+    heap_up(h, 0, pos);
+    return top;
+}
+
+typedef struct {
+    int n;
+    const double *X1, *X2;      /* centred pos1, centred pos2 */
+    double *r1, *r2, *d2, *lb, *rp;
+    int *col;
+} orc_bnb_ws;
+
+/* BranchNodeCluster.calcbounds (bnbAlignment.py:232-277) */
+static void orc_bnb_bounds(orc_bnb_ws *w, orc_bnb_node *nd, double bestupper, int force, double *rpos_out) {
+    const int n = w->n;
+    double M[9];
+    orc_angle_axis(nd->rot, M);
+    double *rp = w->rp;
+    for (int j = 0; j < n; ++j)   /* rpos2 = (sign * pos2) . M, row vectors */
+        for (int c = 0; c < 3; ++c)
+            rp[3 * j + c] = nd->sign * (w->X2[3 * j] * M[c] + w->X2[3 * j + 1] * M[3 + c] + w->X2[3 * j + 2] * M[6 + c]);
+    if (rpos_out) memcpy(rpos_out, rp, sizeof(double) * 3 * n);
+    const double theta = fmin(sqrt(3.0) * nd->width / 2, ORC_PI), cosd = cos(theta), sind = fabs(sin(theta));
+    double upper = 0.0;
+    if (!force) {   /* nearest atom of pos1 to each rotated pos2 atom */
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) {
+            double best = HUGE_VAL;
+            int bi = 0;
+            for (int i = 0; i < n; ++i) {
+                double t = 0;
+                for (int c = 0; c < 3; ++c) {
+                    const double e = w->X1[3 * i + c] - rp[3 * j + c];
+                    t += e * e;
+                }
+                if (t < best) { best = t; bi = i; }
+            }
+            w->col[j] = bi;
+            w->lb[j] = best;
+            s += best;
+        }
+        upper = sqrt(s);
+    }
+    if (force || upper < bestupper) {
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                double t = 0;
+                for (int c = 0; c < 3; ++c) {
+                    const double e = w->X1[3 * i + c] - rp[3 * j + c];
+                    t += e * e;
+                }
+                const double rr = w->r1[i] * w->r2[j], rs = w->r1[i] * w->r1[i] + w->r2[j] * w->r2[j];
+                const double cosa = 0.5 * (rs - t) / rr, sina = sqrt(fmin(fmax(1.0 - cosa * cosa, 0.0), 1.0));
+                const double cdm = (cosa > cosd) ? 1.0 : cosa * cosd + sina * sind;
+                w->d2[(size_t)i * n + j] = t;
+                w->lb[(size_t)i * n + j] = fmax(rs - 2 * rr * cdm, 0.0);
+            }
+        nd->lower = sqrt(orc_lap_dense(n, w->lb, w->col));
+        if (nd->lower < bestupper) {
+            orc_lap_dense(n, w->d2, w->col);
+            double s = 0;
+            for (int i = 0; i < n; ++i)
+                for (int c = 0; c < 3; ++c) {
+                    const double e = w->X1[3 * i + c] - rp[3 * w->col[i] + c];
+                    s += e * e;
+                }
+            nd->upper = sqrt(s);
+        } else {
+            nd->upper = HUGE_VAL;
+        }
+    } else {   /* quick bounds from the nearest neighbours */
+        double s = 0;
+        for (int j = 0; j < n; ++j) {
+            const double r1 = w->r1[w->col[j]], r2 = w->r2[j], dd = w->lb[j];
+            const double cosa = 0.5 * (r1 * r1 + r2 * r2 - dd) / r1 / r2;
+            const double sina = sqrt(fmin(fmax(1.0 - cosa * cosa, 0.0), 1.0));
+            const double cdm = (cosa > cosd) ? 1.0 : cosa * cosd + sina * sind;
+            s += fmax(r1 * r1 + r2 * r2 - 2 * r1 * r2 * cdm, 0.0);
+        }
+        nd->lower = sqrt(s);
+        nd->upper = upper;
+    }
+}
+
+int orc_bnb_cluster(const double *pos1, const double *pos2, int n, int invert, long long niter, double rtol,
+                    double atol, double *dist, double *aligned, long long *nodes_out) {
+    double *X1 = malloc(sizeof(double) * 3 * n), *X2 = malloc(sizeof(double) * 3 * n);
+    double c1[3] = {0, 0, 0}, c2[3] = {0, 0, 0};
+    for (int j = 0; j < n; ++j)
+        for (int c = 0; c < 3; ++c) { c1[c] += pos1[3 * j + c]; c2[c] += pos2[3 * j + c]; }
+    for (int c = 0; c < 3; ++c) { c1[c] /= n; c2[c] /= n; }
+    for (int j = 0; j < n; ++j)
+        for (int c = 0; c < 3; ++c) { X1[3 * j + c] = pos1[3 * j + c] - c1[c]; X2[3 * j + c] = pos2[3 * j + c] - c2[c]; }
+    orc_bnb_ws w;
+    w.n = n; w.X1 = X1; w.X2 = X2;
+    w.r1 = malloc(sizeof(double) * n); w.r2 = malloc(sizeof(double) * n);
+    w.d2 = malloc(sizeof(double) * n * n); w.lb = malloc(sizeof(double) * n * n);
+    w.rp = malloc(sizeof(double) * 3 * n); w.col = malloc(sizeof(int) * n);
+    for (int j = 0; j < n; ++j) {
+        w.r1[j] = sqrt(X1[3 * j] * X1[3 * j] + X1[3 * j + 1] * X1[3 * j + 1] + X1[3 * j + 2] * X1[3 * j + 2]);
+        w.r2[j] = sqrt(X2[3 * j] * X2[3 * j] + X2[3 * j + 1] * X2[3 * j + 1] + X2[3 * j + 2] * X2[3 * j + 2]);
+    }
+    orc_heap h = {NULL, 0, 0};
+    orc_bnb_node start[2];
+    int nstart = invert ? 2 : 1;
+    for (int k = 0; k < nstart; ++k) {
+        orc_bnb_node s0 = {{0, 0, 0}, 2 * ORC_PI, 0, 0, k ? -1 : 1, k};
+        orc_bnb_bounds(&w, &s0, HUGE_VAL, 1, NULL);
+        start[k] = s0;
+    }
+    orc_bnb_node best = start[0];
+    heap_push(&h, start[0]);
+    for (int k = 1; k < nstart; ++k) {
+        if (start[k].upper < best.upper) best = start[k];
+        if (start[k].lower < best.upper) heap_push(&h, start[k]);
+    }
+    long long nodes = 0;
+    int next_id = nstart;
+    while (h.n > 0) {
+        orc_bnb_node nd = heap_pop(&h);
+        ++nodes;
+        if (nd.lower < best.upper - rtol * best.upper - atol) {
+            for (int a = 0; a < 2; ++a)       /* children in numpy.indices order */
+                for (int b = 0; b < 2; ++b)
+                    for (int c = 0; c < 2; ++c) {
+                        orc_bnb_node ch = nd;
+                        const double q = 0.25 * nd.width;
+                        ch.rot[0] = (2 * a - 1) * q + nd.rot[0];
+                        ch.rot[1] = (2 * b - 1) * q + nd.rot[1];
+                        ch.rot[2] = (2 * c - 1) * q + nd.rot[2];
+                        ch.width = 0.5 * nd.width;
+                        ch.id = next_id++;
+                        orc_bnb_bounds(&w, &ch, best.upper, 0, NULL);
+                        if (ch.lower < best.upper) {
+                            if (ch.upper < best.upper) best = ch;
+                            heap_push(&h, ch);
+                        }
+                    }
+            if (nodes > niter) break;
+        }
+    }
+    *dist = best.upper;
+    if (aligned) {   /* best node's rotated pos2, moved onto pos1's centroid */
+        orc_bnb_bounds(&w, &best, HUGE_VAL, 1, aligned);
+        for (int j = 0; j < n; ++j)
+            for (int c = 0; c < 3; ++c) aligned[3 * j + c] += c1[c];
+    }
+    if (nodes_out) *nodes_out = nodes;
+    free(h.a); free(X1); free(X2); free(w.r1); free(w.r2); free(w.d2); free(w.lb); free(w.rp); free(w.col);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* SETWAVEK / PERIODICFOURIERPERM / damping / DOTFOURIERCOEFFS / FFT3D / ABS
  * (fastbulk.f90:414-454,522-523,567-683; fastutils.f90:554-569):
  *   F(k) = sum_s C^B_s(k) conj(C^A_s(k)) exp(-k^2 s^2),

@@ -111,6 +111,16 @@ int    orc_harm_align(const double *pos1, const double *pos2, int n,
 void   orc_calc_similarity(const double *c1, const double *c2, int ngroups, int nmax, int L,
                            double *norm, double *maxover);
 
+/* Branch and bound over rotations (the upstream Python BranchandBoundMaster,
+ * fastoverlap/bnbAlignment.py:23-104,204-277): both structures centred,
+ * best-first search over angle-axis cubes (start width 2 pi, 8 children of
+ * half width) ordered by the lower bound, until the lower bound is within
+ * rtol * best + atol of the best upper bound or `niter` nodes; invert also
+ * starts from -pos2.  dist: the best upper bound; aligned (optional): that
+ * node's rotated pos2 on pos1's centroid, in pos2's order (as upstream). */
+int    orc_bnb_cluster(const double *pos1, const double *pos2, int n, int invert, long long niter,
+                       double rtol, double atol, double *dist, double *aligned, long long *nodes);
+
 /* batch helper for the CPU baseline: runs pairs on nthreads OS threads */
 int    orc_cluster_align_many(int npairs, const double *pos1, const double *pos2,
                               const int64_t *coord_off, const int *natoms,

@@ -326,6 +326,20 @@ def bulk_align_ohcell(pos1, pos2, box, perm=None, sigma=0.0, nwave=0, nfspace=0,
     return best
 
 
+def bnb_cluster(pos1, pos2, invert=True, niter=None, rtol=5e-2, atol=1e-3):
+    """Branch and bound over rotations (upstream BranchandBoundMaster).
+    Returns dict(dist, aligned, nodes)."""
+    p1 = np.ascontiguousarray(pos1, dtype=np.float64).reshape(-1, 3)
+    p2 = np.ascontiguousarray(pos2, dtype=np.float64).reshape(-1, 3)
+    al = np.zeros_like(p1)
+    d = ctypes.c_double()
+    nodes = ctypes.c_longlong()
+    lib().orc_bnb_cluster(_d(p1), _d(p2), len(p1), int(bool(invert)),
+                          ctypes.c_longlong(2 ** 62 if niter is None else int(niter)), ctypes.c_double(rtol),
+                          ctypes.c_double(atol), ctypes.byref(d), _d(al), ctypes.byref(nodes))
+    return dict(dist=d.value, aligned=al, nodes=nodes.value)
+
+
 def cluster_align_many(pairs, nrot=10, invert=True, cutoff=True, nthreads=None):
     """pairs: list of dicts(pos1, pos2, perm, Jmax, sigma). Returns distances."""
     nthreads = nthreads or os.cpu_count() or 1

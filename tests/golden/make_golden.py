@@ -130,9 +130,29 @@ def harm(R=None):
     print("harm", np.round(dists, 9), norm, float(grid.max()))
 
 
+def bnb(R=None):
+    """bnb.npz: the upstream Python branch and bound over rotations
+    (BranchandBoundMaster, default rtol/atol, to completion) on four seeded
+    cluster pairs: distance, expanded node count and aligned coordinates."""
+    R = R or ref_shim.import_reference(os.environ.get("FO_REF_ROOT", "/root/reference"))
+    from fastoverlap import bnbAlignment
+    P1, P2, D, N, A = [], [], [], [], []
+    for k, n in [(5, 13), (6, 16), (7, 20), (8, 13)]:
+        q = synth.cluster_pair(k, n=n)
+        m = bnbAlignment.BranchandBoundMaster()
+        d, _, x2 = m(q["pos1"], q["pos2"])
+        P1.append(q["pos1"]); P2.append(q["pos2"]); D.append(float(d)); N.append(m.nodes); A.append(x2)
+    np.savez(os.path.join(HERE, "bnb.npz"), natoms=np.array([len(x) for x in P1]), pos1=np.concatenate(P1),
+             pos2=np.concatenate(P2), dist=np.array(D), nodes=np.array(N), aligned=np.concatenate(A))
+    print("bnb", D, N)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["harm"]:
         harm()
+    elif sys.argv[1:] == ["bnb"]:
+        bnb()
     else:
         main()
         harm()
+        bnb()

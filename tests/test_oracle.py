@@ -198,3 +198,17 @@ def test_harmonic_alignment_matches_upstream(oracle_mod, golden):
                                   kwidth=0.3, nrot=10, invert=True)
         assert o["status"] == 0
         assert abs(o["dist"] - g["dist_nmax10_j7"][k]) <= 1e-8 * o["dist"]
+
+
+def test_branch_and_bound_matches_upstream(oracle_mod, golden):
+    """The oracle's search over rotations expands the upstream Python's nodes
+    in the same order: same count, distance and aligned coordinates."""
+    g = golden("bnb")
+    off = 0
+    for k, n in enumerate(g["natoms"]):
+        sl = slice(off, off + int(n))
+        o = oracle_mod.bnb_cluster(g["pos1"][sl], g["pos2"][sl])
+        assert o["nodes"] == int(g["nodes"][k])
+        assert abs(o["dist"] - g["dist"][k]) <= 1e-12 * g["dist"][k]
+        assert np.max(np.abs(o["aligned"] - g["aligned"][sl])) <= 1e-12
+        off += int(n)
