@@ -19,10 +19,12 @@ from .batch import (BulkBatch, ClusterBatch, HarmonicClusterBatch, align_cluster
                     findpeaks)
 from .serve import Server  # noqa: F401
 from .periodicAlignment import PeriodicAlign, PeriodicAlignFortran  # noqa: F401
+from .bnbAlignment import BranchandBoundMaster, bnb_align_clusters  # noqa: F401
 from .sphericalAlignment import (SphericalAlign, SphericalAlignFortran, SphericalHarmonicAlign,  # noqa: F401
                                  SphericalHarmonicAlignFortran)
 
 __all__ = ["SphericalAlign", "SphericalAlignFortran", "SphericalHarmonicAlign", "SphericalHarmonicAlignFortran",
-           "HarmonicClusterBatch", "PeriodicAlign", "PeriodicAlignFortran",
+           "HarmonicClusterBatch", "PeriodicAlign", "PeriodicAlignFortran", "BranchandBoundMaster",
+           "bnb_align_clusters",
            "align_clusters", "align_periodic", "ClusterBatch", "BulkBatch", "findpeaks", "Server", "Context",
            "FoError", "default_context", "load"]

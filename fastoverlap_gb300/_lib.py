@@ -103,6 +103,12 @@ EXPORTS = {
     "fo_cluster_plan_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
                                               ctypes.c_int, ctypes.POINTER(_vp)]),
     "fo_plan_set_graph": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fo_bnb_cluster": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
+                                      ctypes.c_double, ctypes.c_double, _dp, _dp,
+                                      ctypes.POINTER(ctypes.c_longlong)]),
+    "fo_bnb_cluster_batch": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, ctypes.c_int, ctypes.c_longlong,
+                                            ctypes.c_double, ctypes.c_double, _dp, _dp,
+                                            ctypes.POINTER(ctypes.c_longlong)]),
     "fo_bulk_plan_create": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
                                            ctypes.c_int, ctypes.POINTER(_vp)]),
     "fo_plan_run": (ctypes.c_int, [_vp]),

@@ -1520,5 +1520,7 @@ void fo_profile_reset(fo_ctx *ctx) {
 namespace fo {
 fo_opts ctx_opts(const fo_ctx *ctx) { return ctx->opts; }
 void ctx_set_budget(fo_ctx *ctx, size_t bytes) { ctx->opts.hbm_budget_bytes = bytes; }
+cudaStream_t ctx_stream(fo_ctx *ctx) { return ctx->stream; }
+fo_status ctx_error(fo_ctx *ctx, fo_status s, const char *msg) { return set_err(ctx, s, "%s", msg); }
 }  // namespace fo
 

@@ -116,5 +116,7 @@ void launch_select(const RefineBuffers &b, cudaStream_t s);
 // context options (library-internal; the server creates worker contexts)
 fo_opts ctx_opts(const fo_ctx *ctx);
 void ctx_set_budget(fo_ctx *ctx, size_t bytes);
+cudaStream_t ctx_stream(fo_ctx *ctx);
+fo_status ctx_error(fo_ctx *ctx, fo_status s, const char *msg);   // sets the message fo_last_error returns
 
 }  // namespace fo

@@ -22,6 +22,8 @@
  *   fo_calc_overlap_matrices <- CLUSTERFASTOVERLAP::CALCOVERLAPMATRICES
  *                             fastoverlap/f90/fastclusters.f90:846-866 (compareList, :622-663)
  *   fo_cluster_harm_*      <- the same harmonic-basis alignment for many pairs
+ *   fo_bnb_cluster(_batch) <- BranchandBoundMaster (branch and bound over rotations),
+ *                             fastoverlap/bnbAlignment.py:23-104,204-277
  *   fo_bulk_align_group    <- BULKFASTOVERLAP::ALIGNGROUP fastoverlap/f90/fastbulk.f90:336-412
  *                             (f2py bulkfastoverlap.aligngroup, periodicAlignment.py:570-605)
  *   fo_cluster_align_batch <- SphericalAlign.__call__ / SphericalAlignFortran.__call__
@@ -304,6 +306,23 @@ fo_status fo_bulk_align_group(fo_ctx *ctx, const double *coords1list, int n1list
                               double boxlx, double boxly, double boxlz, double kwidth,
                               int ndisplacements, int nwave, int nfspace, double *distmat,
                               double *alignedcoords2, int sym);
+
+/* Branch and bound over rotations (the upstream Python BranchandBoundMaster
+ * with BranchNodeCluster): both structures centred; a best-first search over
+ * cubes of angle-axis vectors (start width 2 pi, 8 children of half width)
+ * by lower bound until it is within rtol * best + atol of the best upper
+ * bound, or after niter expanded nodes; invert also starts from -pos2.
+ * dist: the best upper bound (the assignment distance at that node's
+ * rotation); aligned (optional): that node's rotated pos2 on pos1's centroid,
+ * in pos2's atom order; nodes (optional): nodes taken from the queue.  One
+ * species, natoms <= 256.  The batch form runs npairs searches side by side
+ * (pair p's atoms follow pair p-1's in pos1, pos2 and aligned). */
+fo_status fo_bnb_cluster(fo_ctx *ctx, const double *pos1, const double *pos2, int natoms, int invert,
+                         long long niter, double rtol, double atol, double *dist, double *aligned,
+                         long long *nodes);
+fo_status fo_bnb_cluster_batch(fo_ctx *ctx, int npairs, const int *natoms, const double *pos1,
+                               const double *pos2, int invert, long long niter, double rtol, double atol,
+                               double *dist, double *aligned, long long *nodes);
 
 /* BULKFASTOVERLAP::CALCDEFAULTS */
 fo_status fo_bulk_calcdefaults(int natoms, double boxlx, double boxly, double boxlz,
