@@ -170,3 +170,29 @@ def test_batch_result_unpacking_spans():
     assert [x.shape for x in out["aligned"]] == [(3, 3), (5, 3), (2, 3)]
     assert [x.tolist() for x in out["perm"]] == [[0, 1, 2], [3, 4, 5, 6, 7], [8, 9]]
     assert out["aligned"][1][0].tolist() == [9.0, 10.0, 11.0]
+
+
+def test_new_wrappers_refuse_unsupported_arguments_before_any_device_work():
+    import numpy as np
+    import pytest
+    import fastoverlap_gb300 as F
+    from fastoverlap_gb300.sphericalAlignment import _average_separation
+
+    with pytest.raises(NotImplementedError):
+        F.BranchandBoundMaster(initialNodes=[object()])
+    with pytest.raises(NotImplementedError):
+        F.BranchandBoundMaster()(np.zeros((3, 3)), np.zeros((3, 3)), extra_inputs=[1])
+    with pytest.raises(NotImplementedError):
+        F.SphericalHarmonicAlign(scale=0.3).align(np.zeros((3, 3)), np.zeros((3, 3)), calcCoeffs=lambda b: None)
+    # averageSeparation (sphericalAlignment.py:35-41): mean nearest-neighbour distance
+    x = np.array([[0.0, 0, 0], [1.0, 0, 0], [3.0, 0, 0]])
+    assert abs(_average_separation(x) - (1.0 + 1.0 + 2.0) / 3) < 1e-15
+
+
+def test_oracle_cubic_operations_are_the_48_signed_permutations(oracle_mod):
+    import numpy as np
+    Ms = [oracle_mod.oh_operation(k) for k in range(48)]
+    assert np.array_equal(Ms[0], np.eye(3))
+    assert len({tuple(M.ravel()) for M in Ms}) == 48
+    for M in Ms:
+        assert np.array_equal(M @ M.T, np.eye(3)) and set(np.abs(M).sum(0)) == {1.0}
