@@ -288,6 +288,7 @@ struct BnbSearch {
     BnbNode best{};
     long long nodes = 0;
     bool active = true;
+    bool failed = false;   // an assignment of one of its children hit the step guard
 };
 
 }  // namespace
@@ -330,11 +331,24 @@ fo_status fo_bnb_cluster_batch(fo_ctx *ctx, int npairs, const int *natoms, const
             r2[a0[p] + j] = std::sqrt(X2[q] * X2[q] + X2[q + 1] * X2[q + 1] + X2[q + 2] * X2[q + 2]);
         }
     }
-    // device inputs and per-step buffers for up to 8 children per search
+    // device inputs and per-launch buffers for up to maxch children: all the
+    // searches' 8 children at once, or fewer launches' worth when the
+    // context's HBM budget (caller's, else 80% of the free memory) is smaller
     const long long sstride = bnb_stride(maxn);
-    const size_t maxch = 8 * (size_t)npairs;
-    const size_t bytes = (2 * 3 * (size_t)tot + 2 * (size_t)tot) * sizeof(double) + 2 * (size_t)npairs * sizeof(int) +
-                         maxch * (sizeof(BnbChild) + 4 * sizeof(double) + sizeof(int) + sstride * sizeof(double)) + 1024;
+    const size_t fixed = (2 * 3 * (size_t)tot + 2 * (size_t)tot) * sizeof(double) + 2 * (size_t)npairs * sizeof(int) +
+                         16 * 256;
+    const size_t per_child = sizeof(BnbChild) + 4 * sizeof(double) + sizeof(int) + sstride * sizeof(double) + 64;
+    size_t budget = fo::ctx_opts(ctx).hbm_budget_bytes;
+    if (!budget) {
+        size_t fr = 0, tt = 0;
+        cudaMemGetInfo(&fr, &tt);
+        budget = (size_t)(0.8 * fr);
+    }
+    if (budget < fixed + 8 * per_child)
+        return bnb_err(ctx, FO_ERR_OOM_BUDGET, "branch and bound needs %zu bytes, budget %zu", fixed + 8 * per_child,
+                       budget);
+    const size_t maxch = std::min(8 * (size_t)npairs, std::max((size_t)8, (budget - fixed) / per_child));
+    const size_t bytes = fixed + maxch * per_child;
     unsigned char *dm = nullptr;
     fo_status s = bnb_cuda(ctx, cudaMalloc(&dm, bytes), "cudaMalloc");
     if (s) return s;
@@ -358,18 +372,22 @@ fo_status fo_bnb_cluster_batch(fo_ctx *ctx, int npairs, const int *natoms, const
     std::vector<BnbChild> ch;
     std::vector<double> vals;
     std::vector<int> stat;
+    // every child of ch, in launches of at most maxch; stat[k] != 0 marks a
+    // child whose assignment hit its step guard
     auto evaluate = [&]() -> fo_status {
         if (ch.empty()) return FO_OK;
-        cudaMemcpyAsync(dch, ch.data(), ch.size() * sizeof(BnbChild), cudaMemcpyHostToDevice, st);
-        launch_bnb_children(dch, (int)ch.size(), dX1, dX2, dr1, dr2, da0, dn, dscr, sstride, dout, dst, st);
         vals.resize(4 * ch.size());
         stat.resize(ch.size());
-        cudaMemcpyAsync(vals.data(), dout, vals.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(stat.data(), dst, stat.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
-        fo_status e = bnb_cuda(ctx, cudaStreamSynchronize(st), "branch and bound");
-        for (size_t k = 0; !e && k < stat.size(); ++k)
-            if (stat[k]) e = bnb_err(ctx, FO_ERR_LAP_FAILED, "branch and bound: assignment step guard");
-        return e;
+        for (size_t c0 = 0; c0 < ch.size(); c0 += maxch) {
+            const size_t nc = std::min(maxch, ch.size() - c0);
+            cudaMemcpyAsync(dch, ch.data() + c0, nc * sizeof(BnbChild), cudaMemcpyHostToDevice, st);
+            launch_bnb_children(dch, (int)nc, dX1, dX2, dr1, dr2, da0, dn, dscr, sstride, dout, dst, st);
+            cudaMemcpyAsync(vals.data() + 4 * c0, dout, 4 * nc * sizeof(double), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(stat.data() + c0, dst, nc * sizeof(int), cudaMemcpyDeviceToHost, st);
+            fo_status e = bnb_cuda(ctx, cudaStreamSynchronize(st), "branch and bound");
+            if (e) return e;
+        }
+        return FO_OK;
     };
     std::vector<BnbSearch> S(npairs);
     // start nodes, bounds forced: the assignment bounds with no best yet
@@ -378,6 +396,12 @@ fo_status fo_bnb_cluster_batch(fo_ctx *ctx, int npairs, const int *natoms, const
         for (int k = 0; k < nstart; ++k) ch.push_back(BnbChild{{0, 0, 0}, 2 * FO_PI, p, k ? -1 : 1});
     s = evaluate();
     for (int p = 0; !s && p < npairs; ++p) {
+        for (int k = 0; k < nstart; ++k)
+            if (stat[p * nstart + k]) S[p].failed = true;
+        if (S[p].failed) {
+            S[p].active = false;
+            continue;
+        }
         BnbNode st0[2];
         for (int k = 0; k < nstart; ++k) {
             const double *v = &vals[4 * (size_t)(p * nstart + k)];
@@ -419,6 +443,12 @@ fo_status fo_bnb_cluster_batch(fo_ctx *ctx, int npairs, const int *natoms, const
         // the sequential decisions, with the best bound as it moves
         for (size_t o = 0; !s && o < owner.size(); ++o) {
             BnbSearch &q = S[owner[o]];
+            for (int k = 0; k < 8; ++k)
+                if (stat[8 * o + k]) q.failed = true;
+            if (q.failed) {   // this search stops; the others go on
+                q.active = false;
+                continue;
+            }
             for (int k = 0; k < 8; ++k) {
                 const BnbChild &c = ch[8 * o + k];
                 const double *v = &vals[4 * (8 * o + k)];
@@ -441,9 +471,17 @@ fo_status fo_bnb_cluster_batch(fo_ctx *ctx, int npairs, const int *natoms, const
     cudaFree(dm);
     if (s) return s;
     // outputs: the best node's rotated pos2 on pos1's centroid, in pos2's order
+    int nfailed = 0;
     for (int p = 0; p < npairs; ++p) {
-        dist[p] = S[p].best.upper;
         if (nodes) nodes[p] = S[p].nodes;
+        if (S[p].failed) {
+            ++nfailed;
+            dist[p] = NAN;
+            if (aligned)
+                for (int j = 0; j < 3 * natoms[p]; ++j) aligned[3 * (size_t)a0[p] + j] = NAN;
+            continue;
+        }
+        dist[p] = S[p].best.upper;
         if (aligned) {
             const BnbNode &b = S[p].best;
             const double th = std::sqrt(b.rot[0] * b.rot[0] + b.rot[1] * b.rot[1] + b.rot[2] * b.rot[2]);
@@ -464,6 +502,9 @@ fo_status fo_bnb_cluster_batch(fo_ctx *ctx, int npairs, const int *natoms, const
             }
         }
     }
+    if (nfailed)
+        return bnb_err(ctx, FO_ERR_LAP_FAILED, "branch and bound: assignment step guard in %d of %d searches",
+                       nfailed, npairs);
     return FO_OK;
 }
 

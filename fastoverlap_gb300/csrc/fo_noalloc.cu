@@ -17,7 +17,9 @@
 // keeps the previous call's contents, so the product grid is cleared at the
 // start of every call; calls that overlap on the GPU (different streams, or
 // host threads issuing concurrently) race on the array and must be ordered
-// by the caller.
+// by the caller.  The pair and group descriptors reach the array through the
+// parameters of a small kernel (copied at launch), so no host buffer has to
+// outlive the call.
 #include "../../include/fastoverlap_gb300.h"
 #include "fo_common.cuh"
 #include "fo_kernels.h"
@@ -25,7 +27,6 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
-#include <vector>
 
 namespace {
 
@@ -61,6 +62,26 @@ cudaError_t scratch_address(unsigned char **out) {
     return cudaSuccess;
 }
 
+// Descriptors of one call, passed by value to k_noalloc_desc (kernel
+// parameters are copied when the launch is queued).
+struct NoAllocDesc {
+    fo::PairDev pair;
+    fo::GroupDev groups[kNoAllocMaxGroups];
+    int ngroups;
+};
+static_assert(sizeof(NoAllocDesc) <= 4000, "descriptor parameter above the classic launch limit");
+
+// Writes the pair descriptor and the ngroups group descriptors to the head of
+// the scratch array (PairDev, then GroupDev[ngroups]).
+__global__ void k_noalloc_desc(const NoAllocDesc d, unsigned char *dst) {
+    const unsigned char *src = (const unsigned char *)&d.pair;
+    const int pbytes = (int)sizeof(fo::PairDev);
+    const int gbytes = d.ngroups * (int)sizeof(fo::GroupDev);
+    const unsigned char *gsrc = (const unsigned char *)d.groups;
+    for (int i = threadIdx.x; i < pbytes + gbytes; i += blockDim.x)
+        dst[i] = i < pbytes ? src[i] : gsrc[i - pbytes];
+}
+
 int fastlen(int n) {
     if (n <= 1) return 1;
     for (int m = n;; ++m) {
@@ -94,11 +115,15 @@ extern "C" fo_status fo_bulk_overlap_noalloc(const double *d_pos1, const double 
     if (M < 2 * K + 1 || M > kNoAllocMaxM) return FO_ERR_BAD_ARGS;  // scratch holds M <= 64
     const double sigma = kwidth > 0 ? kwidth : std::cbrt(boxlx * boxly * boxlz / natoms) / 3.0;
 
+    // an error left pending by earlier work on this thread is not ours to
+    // clear or to report as this call's: refuse, and leave it for the caller
+    if (cudaPeekAtLastError() != cudaSuccess) return FO_ERR_CUDA;
     unsigned char *base = nullptr;
     if (scratch_address(&base) != cudaSuccess) return FO_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
 
-    fo::PairDev P{};
+    NoAllocDesc desc{};
+    fo::PairDev &P = desc.pair;
     P.n = natoms;
     P.ngroups = ngroups;
     P.group0 = 0;
@@ -111,21 +136,19 @@ extern "C" fo_status fo_bulk_overlap_noalloc(const double *d_pos1, const double 
     P.grid0 = 0;
     P.sigma = sigma;
     for (int k = 0; k < 3; ++k) P.box[k] = box[k];
-    std::vector<unsigned char> desc(sizeof(fo::PairDev) + ngroups * sizeof(fo::GroupDev));
-    memcpy(desc.data(), &P, sizeof P);
+    desc.ngroups = ngroups;
     int off = 0;
     for (int g = 0; g < ngroups; ++g) {
-        fo::GroupDev G{};
+        fo::GroupDev &G = desc.groups[g];
         G.pair = 0;
         G.slot0 = off;  // atoms of group g are the contiguous range [off, off + size)
         G.n = group_sizes[g];
         G.m = group_sizes[g] < fo::kMaxNei ? group_sizes[g] : fo::kMaxNei;
         off += group_sizes[g];
-        memcpy(desc.data() + sizeof P + g * sizeof G, &G, sizeof G);
     }
     unsigned char *d_desc = base, *d_fgrid = base + kNoAllocDescBytes;
-    if (cudaMemcpyAsync(d_desc, desc.data(), desc.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return FO_ERR_CUDA;
+    k_noalloc_desc<<<1, 256, 0, st>>>(desc, d_desc);
+    if (cudaGetLastError() != cudaSuccess) return FO_ERR_CUDA;
     // the product grid must start at zero outside the (2K+1)^3 corner
     if (cudaMemsetAsync(d_fgrid, 0, sizeof(double2) * (size_t)M * M * M, st) != cudaSuccess)
         return FO_ERR_CUDA;
@@ -140,6 +163,7 @@ extern "C" fo_status fo_bulk_overlap_noalloc(const double *d_pos1, const double 
     b.maxK = K;
     b.maxM = M;
     fo::launch_bulk_sf(b, false, st);
+    if (cudaGetLastError() != cudaSuccess) return FO_ERR_CUDA;
     fo::launch_bulk_fft(b, false, st);
     return cudaGetLastError() == cudaSuccess ? FO_OK : FO_ERR_CUDA;
 }

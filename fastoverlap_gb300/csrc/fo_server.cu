@@ -25,6 +25,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 namespace {
@@ -44,6 +45,34 @@ struct Req {
 };
 
 using ReqP = std::unique_ptr<Req>;
+
+// Latency percentiles from a histogram with bins 1% wide on a log scale
+// (1 microsecond up to about 6 hours): bounded memory whatever the run
+// length; a percentile is reported as its bin's geometric centre, within
+// 0.5% of the exact value.
+struct LatencyHist {
+    static constexpr int kBins = 2200;
+    static constexpr double kLo = 1e-3, kRatio = 1.01;
+    std::vector<int64_t> bins = std::vector<int64_t>(kBins, 0);
+    int64_t count = 0;
+    double max_ms = 0.0;
+    void add(double ms) {
+        int b = ms > kLo ? (int)std::floor(std::log(ms / kLo) / std::log(kRatio)) : 0;
+        b = std::min(std::max(b, 0), kBins - 1);
+        ++bins[b];
+        ++count;
+        max_ms = std::max(max_ms, ms);
+    }
+    double pct(double q) const {   // nearest rank
+        int64_t k = (int64_t)std::ceil(q * count), acc = 0;
+        if (k < 1) k = 1;
+        for (int b = 0; b < kBins; ++b) {
+            acc += bins[b];
+            if (acc >= k) return std::min(kLo * std::pow(kRatio, b + 0.5), max_ms);
+        }
+        return max_ms;
+    }
+};
 
 // The checks the plan builders make, without a context (bounds as there).
 fo_status validate(const fo_request &q) {
@@ -86,12 +115,13 @@ struct fo_server {
     std::condition_variable cv_work, cv_done;
     std::deque<ReqP> pending;
     std::unordered_map<int64_t, ReqP> finished;
+    std::unordered_set<int64_t> outstanding;   // issued and not yet collected
     int64_t next_ticket = 1;
     bool stop = false;
     std::vector<std::thread> workers;
     // statistics
     int64_t n_sub = 0, n_done = 0, n_fail = 0, n_batches = 0, n_batched = 0;
-    std::vector<double> lat_ms;
+    LatencyHist lat;
     double busy_ms = 0;
 
     void run_kind(fo_ctx *ctx, std::vector<Req *> &rs, int kind);
@@ -218,7 +248,7 @@ void fo_server::loop(fo_ctx *ctx) {
         ++n_batches;
         n_batched += (int64_t)batch.size();
         for (auto &b : batch) {
-            lat_ms.push_back(std::chrono::duration<double, std::milli>(t1 - b->t_submit).count());
+            lat.add(std::chrono::duration<double, std::milli>(t1 - b->t_submit).count());
             ++n_done;
             if (b->status != FO_OK) ++n_fail;
             const int64_t t = b->ticket;
@@ -280,6 +310,7 @@ fo_status fo_server_submit(fo_server *srv, const fo_request *req, int64_t *ticke
         if ((int64_t)srv->pending.size() >= srv->o.max_queue) return FO_ERR_QUEUE_FULL;
         r->ticket = srv->next_ticket++;
         *ticket = r->ticket;
+        srv->outstanding.insert(r->ticket);
         ++srv->n_sub;
         srv->pending.push_back(std::move(r));
     }
@@ -298,6 +329,8 @@ static fo_status take_result(fo_server *srv, int64_t ticket, fo_pair_result *res
     if (permbest && !r->permbest.empty()) std::copy(r->permbest.begin(), r->permbest.end(), permbest);
     const fo_status s = r->status;
     srv->finished.erase(it);
+    srv->outstanding.erase(ticket);
+    srv->cv_done.notify_all();   // a second waiter on this ticket returns FO_ERR_BAD_ARGS
     return s;
 }
 
@@ -305,7 +338,7 @@ fo_status fo_server_poll(fo_server *srv, int64_t ticket, fo_pair_result *result,
                          int *permbest) {
     if (!srv || ticket <= 0) return FO_ERR_BAD_ARGS;
     std::lock_guard<std::mutex> lk(srv->mu);
-    if (ticket >= srv->next_ticket) return FO_ERR_BAD_ARGS;
+    if (!srv->outstanding.count(ticket)) return FO_ERR_BAD_ARGS;   // never issued, or collected
     return take_result(srv, ticket, result, aligned, permbest);
 }
 
@@ -313,13 +346,15 @@ fo_status fo_server_wait(fo_server *srv, int64_t ticket, double timeout_ms, fo_p
                          double *aligned, int *permbest) {
     if (!srv || ticket <= 0) return FO_ERR_BAD_ARGS;
     std::unique_lock<std::mutex> lk(srv->mu);
-    if (ticket >= srv->next_ticket) return FO_ERR_BAD_ARGS;
-    auto ready = [&] { return srv->finished.count(ticket) > 0; };
+    if (!srv->outstanding.count(ticket)) return FO_ERR_BAD_ARGS;   // never issued, or collected
+    // ready once finished, or when another caller collected it meanwhile
+    auto ready = [&] { return srv->finished.count(ticket) > 0 || !srv->outstanding.count(ticket); };
     if (timeout_ms < 0) {
         srv->cv_done.wait(lk, ready);
     } else if (!srv->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
         return FO_ERR_TIMEOUT;
     }
+    if (!srv->outstanding.count(ticket)) return FO_ERR_BAD_ARGS;
     return take_result(srv, ticket, result, aligned, permbest);
 }
 
@@ -333,16 +368,10 @@ fo_status fo_server_stats_get(fo_server *srv, fo_server_stats *st) {
     st->batches = srv->n_batches;
     st->mean_batch = srv->n_batches ? (double)srv->n_batched / srv->n_batches : 0.0;
     st->busy_ms = srv->busy_ms;
-    if (!srv->lat_ms.empty()) {
-        std::vector<double> v = srv->lat_ms;
-        std::sort(v.begin(), v.end());
-        auto pct = [&](double q) {   // nearest rank
-            size_t k = (size_t)std::ceil(q * v.size());
-            return v[k ? k - 1 : 0];
-        };
-        st->latency_p50_ms = pct(0.50);
-        st->latency_p99_ms = pct(0.99);
-        st->latency_max_ms = v.back();
+    if (srv->lat.count) {
+        st->latency_p50_ms = srv->lat.pct(0.50);
+        st->latency_p99_ms = srv->lat.pct(0.99);
+        st->latency_max_ms = srv->lat.max_ms;
     }
     return FO_OK;
 }

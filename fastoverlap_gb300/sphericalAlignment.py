@@ -79,7 +79,9 @@ class SphericalAlign(object):
 
     def __call__(self, pos1, pos2, perm=None, invert=True, calcCoeffs=None, nrot=10, niter=None):
         """Refines the best `nrot` peaks of each orientation; returns
-        (distance, X1, X2) like the upstream __call__ (sphericalAlignment.py:237-247)."""
+        (distance, X1, X2) like the upstream __call__ (sphericalAlignment.py:237-247).
+        `niter` is accepted and unused, as upstream: that __call__ never reads
+        it either."""
         return self.malign(pos1, pos2, perm, invert, calcCoeffs, nrot)
 
     def align_full(self, pos1, pos2, perm=None, invert=True, nrot=10):

@@ -242,7 +242,9 @@ fo_status fo_findpeaks(fo_ctx *ctx, const double *grid, int n, int npeaks, int w
  * scratch array's address; make that first call before any stream capture.
  * All calls share the array (it keeps the previous contents; the kernel
  * clears what must start at zero): calls that overlap on the GPU race and
- * must be serialised by the caller.                                          */
+ * must be serialised by the caller.  If an error from earlier CUDA work is
+ * pending on the calling thread (cudaPeekAtLastError), the call queues
+ * nothing, returns FO_ERR_CUDA and leaves that error for the caller to read. */
 fo_status fo_bulk_overlap_noalloc(const double *d_pos1, const double *d_pos2, int natoms,
                                   const int *group_sizes, int ngroups, double boxlx,
                                   double boxly, double boxlz, double kwidth, int nwave,
@@ -316,7 +318,11 @@ fo_status fo_bulk_align_group(fo_ctx *ctx, const double *coords1list, int n1list
  * rotation); aligned (optional): that node's rotated pos2 on pos1's centroid,
  * in pos2's atom order; nodes (optional): nodes taken from the queue.  One
  * species, natoms <= 256.  The batch form runs npairs searches side by side
- * (pair p's atoms follow pair p-1's in pos1, pos2 and aligned). */
+ * (pair p's atoms follow pair p-1's in pos1, pos2 and aligned).  The children
+ * of one round are evaluated in launches sized to the context's HBM budget.
+ * A search whose assignment hits its step guard stops with dist (and its
+ * aligned rows) NaN while the others finish; the call then returns
+ * FO_ERR_LAP_FAILED. */
 fo_status fo_bnb_cluster(fo_ctx *ctx, const double *pos1, const double *pos2, int natoms, int invert,
                          long long niter, double rtol, double atol, double *dist, double *aligned,
                          long long *nodes);
@@ -386,7 +392,10 @@ fo_status fo_server_submit(fo_server *srv, const fo_request *req, int64_t *ticke
  * status, with result, aligned (3*natoms, may be NULL) and permbest (natoms,
  * 0-based, may be NULL) filled as by the batch entry points, and the ticket
  * released.  fo_server_wait blocks up to timeout_ms (< 0: no limit) and
- * returns FO_ERR_TIMEOUT when the time runs out.                             */
+ * returns FO_ERR_TIMEOUT when the time runs out.  A ticket that was never
+ * issued, or whose result was already collected (by poll or by another
+ * wait), gives FO_ERR_BAD_ARGS at once.  Latency percentiles in the stats
+ * come from a log-scale histogram with 1% bins (within 0.5%).               */
 fo_status fo_server_poll(fo_server *srv, int64_t ticket, fo_pair_result *result, double *aligned,
                          int *permbest);
 fo_status fo_server_wait(fo_server *srv, int64_t ticket, double timeout_ms, fo_pair_result *result,

@@ -38,7 +38,7 @@ from fastoverlap_gb300 import synth  # noqa: E402
 
 
 def main():
-    root = os.environ.get("FO_REF_ROOT", "/root/reference")
+    root = ref_shim.reference_root()
     R = ref_shim.import_reference(root)
     ex = os.path.join(root, "examples")
 
@@ -106,7 +106,7 @@ def harm(R=None):
     structures -- coefficients, the SO(3) coefficients of a pair with their
     norm and overlap maximum (CALCSIMILARITY's two numbers), and end-to-end
     distances of four seeded 38-atom pairs (nmax 10, Jmax 7)."""
-    R = R or ref_shim.import_reference(os.environ.get("FO_REF_ROOT", "/root/reference"))
+    R = R or ref_shim.import_reference(ref_shim.reference_root())
     nmax, L, hw, kw = 6, 5, 1.0, 0.3
     p = synth.cluster_pair(7, n=20)
     X = p["pos1"] - p["pos1"].mean(0)
@@ -134,7 +134,7 @@ def bnb(R=None):
     """bnb.npz: the upstream Python branch and bound over rotations
     (BranchandBoundMaster, default rtol/atol, to completion) on four seeded
     cluster pairs: distance, expanded node count and aligned coordinates."""
-    R = R or ref_shim.import_reference(os.environ.get("FO_REF_ROOT", "/root/reference"))
+    R = R or ref_shim.import_reference(ref_shim.reference_root())
     from fastoverlap import bnbAlignment
     P1, P2, D, N, A = [], [], [], [], []
     for k, n in [(5, 13), (6, 16), (7, 20), (8, 13)]:

@@ -2,8 +2,8 @@
 
 The upstream code targets older numpy/scipy/munkres APIs.  This module installs
 small in-memory compatibility shims (no file of the upstream tree is modified)
-and imports the package from a read-only checkout given by ``FO_REF_ROOT``
-(default: the checkout next to this repository's build container).  It is used
+and imports the package from a read-only checkout whose path the environment
+variable ``FO_REF_ROOT`` must give (there is no default).  It is used
 only by ``make_golden.py`` to produce the committed fixtures; nothing in the
 library or in the GPU tests imports it.
 
@@ -54,8 +54,16 @@ def install_shims():
     sys.modules["munkres"] = munk
 
 
+def reference_root():
+    """The upstream checkout named by FO_REF_ROOT (required)."""
+    root = os.environ.get("FO_REF_ROOT")
+    if not root:
+        raise RuntimeError("set FO_REF_ROOT to the upstream fastoverlap checkout")
+    return root
+
+
 def import_reference(root=None):
-    root = root or os.environ.get("FO_REF_ROOT", "/root/reference")
+    root = root or reference_root()
     install_shims()
     sys.dont_write_bytecode = True
     if root not in sys.path:
