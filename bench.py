@@ -95,11 +95,13 @@ def c3_run(npairs):
             pass
     out, res = {"pairs": npairs, "atoms": 1000, "jmax": 31, "peaks": 20}, {}
     for prec in ("fp64", "mixed"):
-        ctx = Context(precision=prec)
+        ctx = Context(precision=prec, profile=True)
         b = ClusterBatch(ctx, [p[0] for p in pairs], [p[1] for p in pairs], [p[2] for p in pairs],
                          Jmax=31, scale=0.25, nrot=20).plan()
         b.plan_run()
         b.plan_wait()
+        ctx.profile_reset()
+        ctx.flush_l2(512 << 20)
         ctx.record(0)
         b.plan_run()
         ctx.record(1)
@@ -107,8 +109,10 @@ def c3_run(npairs):
         ms = ctx.elapsed_ms(0, 1)
         res[prec] = b.plan_results(with_coords=True)
         out["%s_pairs_per_s" % prec] = npairs / (ms / 1000.0)
+        out["%s_kernel_ms" % prec] = {k: v[0] / max(1, v[1]) for k, v in ctx.profile().items()}
         b.close()
         ctx.close()
+    out["mixed_over_fp64"] = out["mixed_pairs_per_s"] / out["fp64_pairs_per_s"]
     a, f = res["mixed"], res["fp64"]
     ok = (a["status"] == 0) & (f["status"] == 0)
     out["mixed_vs_fp64_max_rel_dist"] = float(np.max(np.abs(a["dist"][ok] - f["dist"][ok]) / f["dist"][ok]))
@@ -395,16 +399,26 @@ def main():
 
     # plain FP64 forms and accuracy of the mixed form
     cfg_extra = {}
-    ctx64 = F.Context(device=local, precision="fp64", profile=False)
+    # the plain FP64 form batched, timed exactly as `value`: resident plan,
+    # W warm-up runs, K timed runs by CUDA events, L2 flushed before each
+    ctx64 = F.Context(device=local, precision="fp64", profile=True)
     b64 = ClusterBatch(ctx64, pos1, pos2, perms, Jmax=jm, scale=0.3, nrot=10, invert=True).plan()
-    b64.plan_run()
-    b64.plan_wait()
-    t0 = time.time()
-    b64.plan_run()
-    b64.plan_wait()
-    t64 = time.time() - t0
+    for _ in range(args.warmup):
+        b64.plan_run()
+        b64.plan_wait()
+    ctx64.profile_reset()
+    ms64 = []
+    for _ in range(args.steps):
+        ctx64.flush_l2(512 << 20)
+        ctx64.record(0)
+        b64.plan_run()
+        ctx64.record(1)
+        b64.plan_wait()
+        ms64.append(ctx64.elapsed_ms(0, 1))
     r64 = b64.plan_results(with_coords=True)
-    cfg_extra["fp64_batched_pairs_per_s"] = args.npairs / t64
+    cfg_extra["fp64_batched_pairs_per_s"] = args.npairs * args.steps / (sum(ms64) / 1000.0)
+    cfg_extra["fp64_batched_kernel_ms_per_step"] = {k: v[0] / max(1, v[1]) for k, v in ctx64.profile().items()}
+    cfg_extra["mixed_over_fp64_batched"] = value / cfg_extra["fp64_batched_pairs_per_s"]
     ns = min(args.plain_sample, args.npairs)
     tp = time.time()
     for k in range(ns):

@@ -1745,6 +1745,7 @@ typedef struct {
     const int64_t *coord_off, *perm_off;
     const int *natoms, *perm, *gsize, *gsize_off, *ngroups, *L;
     double *dist;
+    int *perm_out;   /* optional: permutations at atom offset coord_off / 3 */
     pthread_mutex_t mu;
 } orc_many_job;
 
@@ -1763,6 +1764,7 @@ static void *orc_many_worker(void *arg) {
                           J->perm + J->perm_off[p], J->gsize + J->gsize_off[p], J->ngroups[p],
                           J->L[p], J->sigma[p], J->nrot, J->invert, J->cutoff, al, pb, &r);
         J->dist[p] = r.dist;
+        if (J->perm_out) memcpy(J->perm_out + J->coord_off[p] / 3, pb, sizeof(int) * n);
         free(al);
         free(pb);
     }
@@ -1775,9 +1777,9 @@ int orc_cluster_align_many(int npairs, const double *pos1, const double *pos2,
                            const int *gsize, const int *gsize_off,
                            const int *ngroups, const int *L,
                            const double *sigma, int nrot, int invert,
-                           int cutoff, int nthreads, double *dist_out) {
+                           int cutoff, int nthreads, double *dist_out, int *perm_out) {
     orc_many_job J = {npairs, 0, nrot, invert, cutoff, pos1, pos2, sigma, coord_off, perm_off,
-                      natoms, perm, gsize, gsize_off, ngroups, L, dist_out};
+                      natoms, perm, gsize, gsize_off, ngroups, L, dist_out, perm_out};
     pthread_mutex_init(&J.mu, NULL);
     if (nthreads < 1) nthreads = 1;
     pthread_t *th = malloc(sizeof(pthread_t) * nthreads);

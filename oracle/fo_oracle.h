@@ -121,14 +121,16 @@ void   orc_calc_similarity(const double *c1, const double *c2, int ngroups, int 
 int    orc_bnb_cluster(const double *pos1, const double *pos2, int n, int invert, long long niter,
                        double rtol, double atol, double *dist, double *aligned, long long *nodes);
 
-/* batch helper for the CPU baseline: runs pairs on nthreads OS threads */
+/* batch helper for the CPU baseline and the tests: runs pairs on nthreads OS
+ * threads; perm_out (optional, NULL for none) receives each pair's best
+ * permutation at atom offset coord_off / 3 */
 int    orc_cluster_align_many(int npairs, const double *pos1, const double *pos2,
                               const int64_t *coord_off, const int *natoms,
                               const int *perm, const int64_t *perm_off,
                               const int *gsize, const int *gsize_off,
                               const int *ngroups, const int *L,
                               const double *sigma, int nrot, int invert,
-                              int cutoff, int nthreads, double *dist_out);
+                              int cutoff, int nthreads, double *dist_out, int *perm_out);
 
 #ifdef __cplusplus
 }

@@ -340,8 +340,9 @@ def bnb_cluster(pos1, pos2, invert=True, niter=None, rtol=5e-2, atol=1e-3):
     return dict(dist=d.value, aligned=al, nodes=nodes.value)
 
 
-def cluster_align_many(pairs, nrot=10, invert=True, cutoff=True, nthreads=None):
-    """pairs: list of dicts(pos1, pos2, perm, Jmax, sigma). Returns distances."""
+def cluster_align_many(pairs, nrot=10, invert=True, cutoff=True, nthreads=None, with_perm=False):
+    """pairs: list of dicts(pos1, pos2, perm, Jmax, sigma). Returns distances,
+    and with_perm the list of best permutations too."""
     nthreads = nthreads or os.cpu_count() or 1
     p1 = np.ascontiguousarray(np.concatenate([np.asarray(p["pos1"], float).ravel() for p in pairs]))
     p2 = np.ascontiguousarray(np.concatenate([np.asarray(p["pos2"], float).ravel() for p in pairs]))
@@ -367,8 +368,13 @@ def cluster_align_many(pairs, nrot=10, invert=True, cutoff=True, nthreads=None):
     L = np.ascontiguousarray([p["Jmax"] for p in pairs], np.int32)
     sg = np.ascontiguousarray([p["sigma"] for p in pairs], np.float64)
     out = np.zeros(len(pairs))
+    pout = np.zeros(int(natoms.sum()), np.int32) if with_perm else None
     lib().orc_cluster_align_many(len(pairs), _d(p1), _d(p2), coff.ctypes.data_as(_lp),
                                  _i(natoms), _i(flat), poff.ctypes.data_as(_lp), _i(gs),
                                  _i(goff), _i(ng), _i(L), _d(sg), int(nrot), int(bool(invert)),
-                                 int(bool(cutoff)), int(nthreads), _d(out))
+                                 int(bool(cutoff)), int(nthreads), _d(out),
+                                 _i(pout) if with_perm else None)
+    if with_perm:
+        ao = np.concatenate([[0], np.cumsum(natoms)])
+        return out, [pout[ao[k]:ao[k + 1]].copy() for k in range(len(pairs))]
     return out

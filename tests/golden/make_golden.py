@@ -23,6 +23,20 @@ Fixtures:
               linear assignment (the scipy solver behind the munkres shim).
   e2e.npz     SphericalAlign / PeriodicAlign distances on seeded synthetic
               pairs of the 38-atom and 256-atom configurations.
+  e2e_perm.npz  the same classes on 32 seeded 38-atom pairs and 8 seeded
+              256-atom periodic pairs: distance, aligned coordinates,
+              permutation and overlap maxima (both orientations of the
+              spherical pair; the periodic |F| maximum).
+  peaks.npz   upstream findPeaks (fastoverlap/utils.py:366-396) on seeded
+              overlap grids: 12 inverse-SOFT grids of 38-atom pairs (16^3) and
+              4 periodic |F| grids of 256-atom pairs (32^3); the grids are
+              recomputed by the tests.
+  bessel_c3.npz  upstream calcSO3Coeffs (no cutoff) of a 100-atom pair in a
+              ball of radius 5.65 at sigma 0.25, Jmax 31: the large-argument
+              regime of i_l (x up to about 280) of the 1000-atom study
+              (slices l = 0, 1, 15, 30, 31).
+
+  python tests/golden/make_golden.py [harm|bnb|more]
 """
 import os
 import sys
@@ -147,12 +161,125 @@ def bnb(R=None):
     print("bnb", D, N)
 
 
+def _fixed_periodic(R):
+    class Fixed(R.per.PeriodicAlign):
+        """The upstream periodic class with its cost matrix transposed to the
+        orientation find_best_permutation expects (see blj256.npz)."""
+        def cost_matrix(self, X1, X2):
+            return R.per.PeriodicAlign.cost_matrix(self, X1, X2).T
+    return Fixed
+
+
+def _perm_from_radii(X2, Y):
+    """Atom order of an aligned copy of Y: an alignment moves Y rigidly about
+    its centroid (rotation, maybe inversion), which keeps each atom's distance
+    to the centroid, so row i of X2 came from the atom of Y with the same
+    radius (the radii of a random structure differ)."""
+    ry = np.linalg.norm(Y - Y.mean(0), axis=1)
+    rx = np.linalg.norm(X2 - X2.mean(0), axis=1)
+    d = np.abs(rx[:, None] - ry[None, :])
+    perm = d.argmin(1)
+    srt = np.sort(d, axis=1)
+    return perm, float(srt[:, 0].max()), float(srt[:, 1].min())
+
+
+def e2e_perm(R=None):
+    R = R or ref_shim.import_reference(ref_shim.reference_root())
+    Fixed = _fixed_periodic(R)
+    c0 = dict(dist=[], aligned=[], perm=[], omax=[], omax_inv=[])
+    for k in range(32):
+        p = synth.config0(seed_offset=k)
+        sa = R.sph.SphericalAlign(0.3, 7)
+        d, X1, X2 = sa(p["pos1"], p["pos2"])
+        perm, err, gap = _perm_from_radii(X2, p["pos2"])
+        assert err < 1e-8 < gap, (k, err, gap)
+        Y1, Y2 = sa.COM_shift(p["pos1"], p["pos2"])
+        om = sa.soft.iSOFT(sa.calcSO3Coeffs(Y1, Y2)).real.max()
+        omi = sa.soft.iSOFT(sa.calcSO3Coeffs(Y1, -Y2)).real.max()
+        c0["dist"].append(float(np.real(d)))
+        c0["aligned"].append(np.real(X2))
+        c0["perm"].append(perm)
+        c0["omax"].append(float(om))
+        c0["omax_inv"].append(float(omi))
+    c1 = dict(dist=[], aligned=[], perm=[], omax=[], disp=[])
+    for k in range(8):
+        p = synth.config1(seed_offset=k)
+        pa = Fixed(256, p["box"], p["perm"], scale=0.2, n=7)
+        d, X1, X2, perm, disp = pa(p["pos1"], p["pos2"], npeaks=10)
+        c1["dist"].append(float(d))
+        c1["aligned"].append(X2)
+        c1["perm"].append(np.asarray(perm))
+        c1["omax"].append(float(pa.fabs.max()))
+        c1["disp"].append(np.asarray(disp))
+    np.savez(os.path.join(HERE, "e2e_perm.npz"), c0_seed_offsets=np.arange(32),
+             **{"c0_" + k: np.array(v) for k, v in c0.items()},
+             c1_seed_offsets=np.arange(8), **{"c1_" + k: np.array(v) for k, v in c1.items()})
+    print("e2e_perm c0", np.round(c0["dist"], 4), "c1", np.round(c1["dist"], 4))
+
+
+def peaks(R=None):
+    """Upstream findPeaks on the overlap grids of seeded pairs.  The grids
+    themselves are not stored: the tests recompute them (oracle or GPU), which
+    agree with the upstream grids to 1e-12 (stages.npz pins that)."""
+    R = R or ref_shim.import_reference(ref_shim.reference_root())
+    Fixed = _fixed_periodic(R)
+    kinds, seeds, pk, npk = [], [], [], []
+    grids = []
+    for k in range(12):
+        p = synth.config0(seed_offset=k)
+        sa = R.sph.SphericalAlign(0.3, 7)
+        X1, X2 = sa.COM_shift(p["pos1"], p["pos2"])
+        grids.append(sa.soft.iSOFT(sa.calcSO3Coeffs(X1, X2)).real)
+        kinds.append(0)
+        seeds.append(k)
+    for k in range(4):
+        p = synth.config1(seed_offset=k)
+        pa = Fixed(256, p["box"], p["perm"], scale=0.2, n=7)
+        pa.setPos(p["pos1"], p["pos2"])
+        grids.append(pa.fabs.copy())
+        kinds.append(1)
+        seeds.append(k)
+    for g in grids:
+        q = np.asarray(R.utils.findPeaks(g, npeaks=10, width=2)[0]).reshape(-1, 3)
+        npk.append(len(q))
+        pk.append(np.vstack([q, np.full((10 - len(q), 3), np.nan)]))
+    np.savez(os.path.join(HERE, "peaks.npz"), kind=np.array(kinds), seed_offset=np.array(seeds),
+             peaks=np.array(pk), npeaks=np.array(npk))
+    print("peaks found", npk)
+
+
+def bessel_c3(R=None):
+    """Upstream calcSO3Coeffs in the large-argument regime; the slices
+    l = 0, 1, 15, 30, 31 of the coefficients are kept (the others are formed
+    by the same code path)."""
+    R = R or ref_shim.import_reference(ref_shim.reference_root())
+    p = synth.cluster_pair(31, n=100, radius=5.65, dmin=0.75)
+    X1 = p["pos1"] - p["pos1"].mean(0)
+    X2 = p["pos2"] - p["pos2"].mean(0)
+    sa = R.sph.SphericalAlign(0.25, 31)
+    c = sa.calcSO3Coeffs(X1, X2)
+    ls = np.array([0, 1, 15, 30, 31])
+    r1, r2 = np.linalg.norm(X1, axis=1), np.linalg.norm(X2, axis=1)
+    np.savez(os.path.join(HERE, "bessel_c3.npz"), A=X1, B=X2, sigma=0.25, L=31, ls=ls, coeffs=c[ls],
+             xmax=float(r1.max() * r2.max() / (2 * 0.25 ** 2)))
+    print("bessel_c3 x max", r1.max() * r2.max() / (2 * 0.25 ** 2))
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["harm"]:
         harm()
     elif sys.argv[1:] == ["bnb"]:
         bnb()
+    elif sys.argv[1:] == ["more"]:
+        R = ref_shim.import_reference(ref_shim.reference_root())
+        e2e_perm(R)
+        peaks(R)
+        bessel_c3(R)
     else:
         main()
         harm()
         bnb()
+        R = ref_shim.import_reference(ref_shim.reference_root())
+        e2e_perm(R)
+        peaks(R)
+        bessel_c3(R)

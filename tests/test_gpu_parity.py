@@ -115,10 +115,12 @@ def test_config2_batch_mixed(fo, oracle_mod):
     and identical permutations on >= 99.9% of pairs (all, at this size)."""
     ps = synth.config2(48, seed_offset=500)
     out = _batch(fo, ps, "mixed")
-    od = oracle_mod.cluster_align_many(ps)
+    od, operm = oracle_mod.cluster_align_many(ps, with_perm=True)
     rel = np.abs(out["dist"] - od) / od
     assert np.all(out["status"] == 0)
     assert rel.max() <= 1e-5
+    same = [np.array_equal(a, b) for a, b in zip(out["perm"], operm)]
+    assert np.mean(same) >= 0.999
 
 
 def test_batch_equals_single_pairs(fo):

@@ -1,0 +1,130 @@
+"""GPU results pinned to the reference's own outputs and to FP64 oracle
+fixtures of the large-bandwidth configuration.
+
+  e2e_perm.npz  upstream SphericalAlign / PeriodicAlign on 32 seeded 38-atom
+                pairs and 8 seeded 256-atom periodic pairs: permutation,
+                distance, aligned coordinates, overlap maximum
+  peaks.npz     upstream findPeaks on the overlap grids of seeded pairs
+  c3.npz        the oracle on 1000-atom (800:200) and 300-atom (240:60)
+                clusters at Jmax 31, sigma 0.25, 20 peaks, inversion
+
+Tolerances: FP64 (plain form) 1e-8 relative on distances and overlap maxima
+with identical permutations; mixed form 1e-5 relative with identical
+permutations.
+"""
+import numpy as np
+import pytest
+
+from fastoverlap_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _c0_batch(fo, g, prec, cutoff):
+    ps = [synth.config0(int(k)) for k in g["c0_seed_offsets"]]
+    ctx = fo.Context(precision=prec, cutoff=cutoff)
+    b = fo.ClusterBatch(ctx, [p["pos1"] for p in ps], [p["pos2"] for p in ps], [p["perm"] for p in ps],
+                        Jmax=7, scale=0.3, nrot=10, invert=True)
+    out = b.run()
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("cutoff", [False, True])
+def test_spherical_fp64_matches_upstream(fo, golden, cutoff):
+    g = golden("e2e_perm")
+    out = _c0_batch(fo, g, "fp64", cutoff)
+    assert np.all(out["status"] == 0)
+    for k in range(len(g["c0_seed_offsets"])):
+        assert np.array_equal(out["perm"][k], g["c0_perm"][k]), k
+        assert abs(out["dist"][k] - g["c0_dist"][k]) <= 1e-8 * g["c0_dist"][k]
+        al, ref = out["aligned"][k], g["c0_aligned"][k]
+        assert np.abs((al - al.mean(0)) - (ref - ref.mean(0))).max() <= 1e-8 * np.abs(ref).max()
+        if not cutoff:   # upstream Python forms the coefficients without the 4 sigma cutoff
+            r = out["result"][k]
+            om = g["c0_omax_inv"][k] if r["inverted"] else g["c0_omax"][k]
+            assert abs(r["overlap_max"] - om) <= 1e-8 * abs(om)
+
+
+def test_spherical_mixed_matches_upstream(fo, golden):
+    g = golden("e2e_perm")
+    out = _c0_batch(fo, g, "mixed", False)
+    assert np.all(out["status"] == 0)
+    for k in range(len(g["c0_seed_offsets"])):
+        assert np.array_equal(out["perm"][k], g["c0_perm"][k]), k
+        assert abs(out["dist"][k] - g["c0_dist"][k]) <= 1e-5 * g["c0_dist"][k]
+        r = out["result"][k]
+        om = g["c0_omax_inv"][k] if r["inverted"] else g["c0_omax"][k]
+        assert abs(r["overlap_max"] - om) <= 1e-5 * abs(om)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 1e-5)])
+def test_periodic_matches_upstream(fo, golden, prec, tol):
+    g = golden("e2e_perm")
+    ps = [synth.config1(int(k)) for k in g["c1_seed_offsets"]]
+    ctx = fo.Context(precision=prec)
+    out = fo.BulkBatch(ctx, [p["pos1"] for p in ps], [p["pos2"] for p in ps], [p["box"] for p in ps],
+                       [p["perm"] for p in ps], scale=0.2, nwave=7, ndisps=10).run()
+    ctx.close()
+    assert np.all(out["status"] == 0)
+    for k in range(len(ps)):
+        assert np.array_equal(out["perm"][k], g["c1_perm"][k]), k
+        assert abs(out["dist"][k] - g["c1_dist"][k]) <= tol * g["c1_dist"][k]
+        assert abs(out["result"][k]["overlap_max"] - g["c1_omax"][k]) <= tol * g["c1_omax"][k]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_findpeaks_against_upstream_findpeaks(fo, golden, peak_agreement, prec):
+    """fo_findpeaks on the GPU-computed grids against upstream findPeaks, with
+    the bounds of the oracle's own test (the first peak within 2e-3 cells for
+    spherical grids, 1e-5 periodic; FP32 fits 5e-3 and 1e-4), see
+    tests/test_oracle.py."""
+    from fastoverlap_gb300.batch import bulk_overlap, cluster_overlap, findpeaks
+    g = golden("peaks")
+    ctx = fo.Context(precision=prec, cutoff=False)
+    covs = []
+    for kind, seed, ref, nref in zip(g["kind"], g["seed_offset"], g["peaks"], g["npeaks"]):
+        if kind == 0:
+            p = synth.config0(int(seed))
+            _, grid = cluster_overlap(p["pos1"], p["pos2"], Jmax=7, scale=0.3, ctx=ctx)
+        else:
+            p = synth.config1(int(seed))
+            grid = bulk_overlap(p["pos1"], p["pos2"], p["box"], perm=p["perm"], scale=0.2, nwave=7,
+                                ctx=ctx)
+        pk, _ = findpeaks(grid, 10, 2, ctx=ctx)
+        first, cov = peak_agreement(pk, ref, int(nref), grid.shape[0])
+        lim = (2e-3 if kind == 0 else 1e-5) if prec == "fp64" else (5e-3 if kind == 0 else 1e-4)
+        assert first <= lim, (kind, seed, first)
+        assert cov >= 0.7
+        if nref == 10:
+            assert len(pk) == 10
+        covs.append(cov)
+    ctx.close()
+    assert np.mean(covs) >= 0.9
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 1e-5)])
+def test_large_bandwidth_against_oracle_fixture(fo, golden, prec, tol):
+    """The 1000-atom Jmax-31 configuration (and 300-atom pairs of the same
+    form) against FP64 oracle results: distances within tol relative,
+    identical permutations, the same inversion choice."""
+    g = golden("c3")
+    n = g["natoms"]
+    off = np.concatenate([[0], np.cumsum(n)])
+    pos1 = [g["pos1"][off[k]:off[k + 1]] for k in range(len(n))]
+    pos2 = [g["pos2"][off[k]:off[k + 1]] for k in range(len(n))]
+    perms = []
+    for k in range(len(n)):
+        s = g["sizes"][k]
+        perms.append([np.arange(s[0]), np.arange(s[0], s[0] + s[1])])
+    ctx = fo.Context(precision=prec)
+    out = fo.ClusterBatch(ctx, pos1, pos2, perms, Jmax=int(g["jmax"]), scale=float(g["sigma"]),
+                          nrot=int(g["nrot"]), invert=True).run()
+    ctx.close()
+    assert np.all(out["status"] == 0)
+    for k in range(len(n)):
+        assert np.array_equal(out["perm"][k], g["perm"][off[k]:off[k + 1]]), k
+        assert abs(out["dist"][k] - g["dist"][k]) <= tol * g["dist"][k]
+        assert bool(out["result"][k]["inverted"]) == bool(g["inverted"][k])
+        al, ref = out["aligned"][k], g["aligned"][off[k]:off[k + 1]]
+        assert np.abs(al - ref).max() <= max(tol, 1e-7) * np.abs(ref).max()
