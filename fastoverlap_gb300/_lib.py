@@ -96,6 +96,7 @@ EXPORTS = {
     "fo_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "fo_last_error": (ctypes.c_char_p, [_vp]),
     "fo_set_precision": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fo_set_tensor_cores": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fo_cluster_align_batch": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
                                               ctypes.c_int, _dp, _ip, _vp]),
     "fo_bulk_align_batch": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
@@ -224,7 +225,8 @@ def vp(a):
 class Context(object):
     """Owns one fo_ctx (CUDA stream, Wigner-table cache) on one device."""
 
-    def __init__(self, device=0, precision="fp64", cutoff=True, hbm_budget_bytes=0, profile=False):
+    def __init__(self, device=0, precision="fp64", cutoff=True, hbm_budget_bytes=0, profile=False,
+                 tensor_cores=True):
         self.lib = load()
         opts = FoOpts(device=device, precision=_prec(precision),
                       hbm_budget_bytes=int(hbm_budget_bytes), cutoff=int(bool(cutoff)),
@@ -236,6 +238,8 @@ class Context(object):
         track("contexts", self)
         self.h = h
         self.precision = precision
+        if not tensor_cores:
+            self.set_tensor_cores(False)
 
     def close(self):
         if getattr(self, "h", None):
@@ -256,6 +260,10 @@ class Context(object):
     def set_precision(self, precision):
         self.check(self.lib.fo_set_precision(self.h, _prec(precision)))
         self.precision = precision
+
+    def set_tensor_cores(self, on):
+        """Mixed form: Wigner contraction on the tcgen05 tensor cores (default) or not."""
+        self.check(self.lib.fo_set_tensor_cores(self.h, int(bool(on))))
 
     def profile(self):
         cap = 32

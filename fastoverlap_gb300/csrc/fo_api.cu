@@ -35,13 +35,13 @@ int fastlen(int n) {
     }
 }
 
-const int kNumKernels = 16;
+const int kNumKernels = 17;
 const char *kKernelNames[kNumKernels] = {
     "sph_center", "sph_ylm",    "sph_radial", "sph_coeff", "isoft",      "findpeaks",
     "refine",     "select",     "bulk_prep",  "bulk_sf",   "bulk_fft",   "memset",
-    "wigner",     "h2d",        "d2h",        "other"};
+    "wigner",     "h2d",        "d2h",        "other",     "wigner_tc"};
 enum KId { K_CENTER, K_YLM, K_RADIAL, K_COEFF, K_ISOFT, K_PEAKS, K_REFINE, K_SELECT, K_BPREP,
-           K_BSF, K_BFFT, K_MEMSET, K_WIGNER, K_H2D, K_D2H, K_OTHER };
+           K_BSF, K_BFFT, K_MEMSET, K_WIGNER, K_H2D, K_D2H, K_OTHER, K_WTC };
 
 }  // namespace
 
@@ -50,6 +50,8 @@ struct fo_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     std::map<int, std::pair<double *, float *>> dtab;
+    int tc = 1;   // mixed form: Wigner contraction on the tensor cores
+    std::map<int, std::pair<float *, CUtensorMap>> dtc;   // per bandwidth: its tables in the MMA layout
     double **d_dtab64 = nullptr;
     float **d_dtab32 = nullptr;
     std::vector<int> permgroup, npermsize;
@@ -95,6 +97,10 @@ struct fo_plan {
     std::vector<cudaEvent_t> evs;
     std::vector<int> ev_kid;
     std::vector<fo::RefineBucket> buckets;
+    bool tc = false;         // Wigner contraction on the tensor cores
+    fo::TcBuffers tcb;
+    std::vector<unsigned char> tc_meta;         // tiles, items, pair map (host copy, uploaded once)
+    size_t tc_off_items = 0, tc_off_pmap = 0;   // their offsets in tc_meta (tiles at 0)
 };
 
 namespace {
@@ -154,6 +160,24 @@ fo_status ensure_dtabs(fo_ctx *ctx, const std::vector<int> &bws) {
                                         cudaMemcpyHostToDevice, ctx->stream), "copy");
     if (s) return s;
     return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "wigner tables");
+}
+
+// the tensor-core layout of the Wigner tables of these bandwidths (after
+// ensure_dtabs: built from the FP64 tables) and their tensor maps
+fo_status ensure_tc_tables(fo_ctx *ctx, const std::vector<int> &bws) {
+    for (int bw : bws) {
+        if (ctx->dtc.count(bw)) continue;
+        float *t = nullptr;
+        fo_status s = cuda_check(ctx, cudaMalloc(&t, fo::tc_table_floats(bw) * sizeof(float)), "cudaMalloc(tc table)");
+        if (s) return s;
+        CUtensorMap map;
+        if (!fo::tc_make_table(bw, ctx->dtab[bw].first, t, &map, ctx->stream)) {
+            cudaFree(t);
+            return set_err(ctx, FO_ERR_CUDA, "tensor-map encoder unavailable (driver entry point)");
+        }
+        ctx->dtc.emplace(bw, std::make_pair(t, map));
+    }
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "tensor-core Wigner tables");
 }
 
 // validate the permutation groups of one pair and fill slot2orig
@@ -391,10 +415,17 @@ void fo_ctx_destroy(fo_ctx *ctx) {
     }
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     for (auto &kv : ctx->dtab) { cudaFree(kv.second.first); cudaFree(kv.second.second); }
+    for (auto &kv : ctx->dtc) cudaFree(kv.second.first);
     cudaFree(ctx->d_dtab64);
     cudaFree(ctx->d_dtab32);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+fo_status fo_set_tensor_cores(fo_ctx *ctx, int on) {
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    ctx->tc = on ? 1 : 0;
+    return FO_OK;
 }
 
 fo_status fo_set_precision(fo_ctx *ctx, int precision) {
@@ -408,7 +439,8 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
                                    const std::vector<int> &slot2orig, const std::vector<int> &slot2pair,
                                    const std::vector<int> &cand2pair, const std::vector<int> &cand_list,
                                    size_t ylm_n, size_t w_n,
-                                   size_t coef_n, size_t grid_n, size_t fgrid_n, long long lap_total) {
+                                   size_t coef_n, size_t grid_n, size_t fgrid_n, long long lap_total,
+                                   size_t tc_meta_bytes = 0, size_t tc_s_floats = 0) {
     const size_t T = pl->fp32 ? 4 : 8;
     const int np = pl->npairs, ns = pl->nslots, nc = pl->ncand;
     Carve cv;
@@ -435,6 +467,8 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     size_t o_res = cv.take<fo_pair_result>(np), o_al = cv.take<double>(3 * (size_t)ns),
            o_pb = cv.take<int>(ns);
     size_t o_hd = cv.take<double>(pl->harm_d);
+    size_t o_tcm = cv.take<unsigned char>(tc_meta_bytes), o_tcs = cv.take<float>(tc_s_floats),
+           o_tce = cv.take<int>(tc_meta_bytes ? 1 : 0);
     fo_status s = finish_plan_alloc(ctx, pl, cv.off);
     if (s) return s;
     unsigned char *m = pl->dmem;
@@ -448,6 +482,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     cudaMemcpyAsync(P(o_clist), cand_list.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(P(o_pos1), pos1, 3 * (size_t)ns * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(P(o_pos2), pos2, 3 * (size_t)ns * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (tc_meta_bytes) cudaMemcpyAsync(P(o_tcm), pl->tc_meta.data(), tc_meta_bytes, cudaMemcpyHostToDevice, st);
     s = cuda_check(ctx, cudaStreamSynchronize(st), "plan upload");
     if (s) return s;
 
@@ -527,6 +562,20 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     r.bulk = pl->bulk;
     pl->d_pstatus = r.pstatus;
     pl->d_npeaks = r.npeaks;
+    if (tc_meta_bytes) {
+        fo::TcBuffers &t = pl->tcb;
+        unsigned char *mb = (unsigned char *)P(o_tcm);
+        t.tiles = (const fo::TcTile *)mb;
+        t.items = (const fo::TcItem *)(mb + pl->tc_off_items);
+        t.pmap = (const fo::TcPairMap *)(mb + pl->tc_off_pmap);
+        t.pairs = pl->sb.pairs;
+        t.coef = pl->sb.coef;
+        t.grid = pl->sb.grid;
+        t.S = (float *)P(o_tcs);
+        t.err = (int *)P(o_tce);
+        t.npairs = np;
+        t.maxG = pl->maxG;
+    }
     return FO_OK;
 }
 
@@ -543,6 +592,77 @@ static bool packed_in_order(const PairT *pairs, int npairs) {
     }
     return true;
 }
+}
+
+// Tiles of the tensor-core contraction: the plan's pairs sorted by Jmax
+// (stable), 64 per tile; work items of kTcChunk (m1, m2) combinations; launch
+// groups of at most kTcMaxBuckets bandwidths.  Fills pl->tc_meta (tiles,
+// items, pair map) and pl->tcb.launches and returns the floats of the sum
+// buffer S.
+static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
+    const int np = pl->npairs;
+    std::vector<int> order(np);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pl->hp[a].L < pl->hp[b].L; });
+    std::vector<fo::TcTile> tiles;
+    std::vector<fo::TcItem> items;
+    std::vector<fo::TcPairMap> pmap(np);
+    std::vector<int> tile_L;
+    size_t sfl = 0;
+    for (int a = 0; a < np;) {
+        const int L = pl->hp[order[a]].L;
+        int b = a;
+        while (b < np && pl->hp[order[b]].L == L) ++b;
+        const int G = 2 * (L + 1), W2 = (2 * L + 1) * (2 * L + 1), W2p = ((W2 + 3) / 4) * 4;
+        for (int t0 = a; t0 < b; t0 += fo::kTcTile) {
+            fo::TcTile T{};
+            T.L = L;
+            T.npairs = std::min(fo::kTcTile, b - t0);
+            T.s0 = (long long)sfl;
+            for (int i = 0; i < T.npairs; ++i) {
+                T.coef0[i] = pl->hp[order[t0 + i]].coef0;
+                pmap[order[t0 + i]] = fo::TcPairMap{(long long)sfl, i, 0};
+            }
+            sfl += 2ull * G * 128 * W2p;
+            tiles.push_back(T);
+            tile_L.push_back(L);
+        }
+        a = b;
+    }
+    // launch groups over the distinct bandwidths, in increasing order
+    std::vector<int> Ls(tile_L);
+    Ls.erase(std::unique(Ls.begin(), Ls.end()), Ls.end());
+    pl->tcb.launches.clear();
+    for (size_t g0 = 0; g0 < Ls.size(); g0 += fo::kTcMaxBuckets) {
+        fo::TcLaunch lg{};
+        lg.item0 = (int)items.size();
+        lg.nrmax = 0;
+        const size_t g1 = std::min(Ls.size(), g0 + fo::kTcMaxBuckets);
+        for (size_t bi = g0; bi < g1; ++bi) {
+            const int bw = Ls[bi] + 1;
+            lg.maps.map[bi - g0] = ctx->dtc[bw].second;
+            lg.maps.nr[bi - g0] = fo::tc_rows(bw);
+            lg.nrmax = std::max(lg.nrmax, fo::tc_rows(bw));
+            for (size_t t = 0; t < tiles.size(); ++t) {
+                if (tile_L[t] != Ls[bi]) continue;
+                tiles[t].bucket = (int)(bi - g0);
+                const int W2 = (2 * Ls[bi] + 1) * (2 * Ls[bi] + 1);
+                for (int m0 = 0; m0 < W2; m0 += fo::kTcChunk)
+                    items.push_back(fo::TcItem{(int)t, m0, std::min(W2, m0 + fo::kTcChunk), 0});
+            }
+        }
+        lg.nitems = (int)items.size() - lg.item0;
+        pl->tcb.launches.push_back(lg);
+    }
+    const size_t bt = tiles.size() * sizeof(fo::TcTile);
+    pl->tc_off_items = align256(bt);
+    pl->tc_off_pmap = pl->tc_off_items + align256(items.size() * sizeof(fo::TcItem));
+    pl->tc_meta.assign(pl->tc_off_pmap + pmap.size() * sizeof(fo::TcPairMap), 0);
+    memcpy(pl->tc_meta.data(), tiles.data(), bt);
+    memcpy(pl->tc_meta.data() + pl->tc_off_items, items.data(), items.size() * sizeof(fo::TcItem));
+    memcpy(pl->tc_meta.data() + pl->tc_off_pmap, pmap.data(), pmap.size() * sizeof(fo::TcPairMap));
+    pl->tc = true;
+    return sfl;
 }
 
 // harm_n < 0: the Gaussian-kernel coefficients of ALIGN; harm_n >= 0: the
@@ -658,11 +778,18 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
     bws.erase(std::unique(bws.begin(), bws.end()), bws.end());
     fo_status s = ensure_dtabs(ctx, bws);
     if (s) { delete pl; return s; }
+    size_t tc_s = 0;
+    if (pl->fp32 && ctx->tc) {
+        s = ensure_tc_tables(ctx, bws);
+        if (s) { delete pl; return s; }
+        tc_s = tc_plan_layout(ctx, pl);
+    }
     build_buckets(pl, rassign, cand_list);
     pl->harm_n = harm_n >= 0 ? harm_n : -1;
     pl->harm_d = harm_n >= 0 ? 2 * (size_t)pl->nslots * (harm_n + 1) * (pl->maxL + 1) : 0;
     s = plan_common_alloc(ctx, pl, contig ? pos1 : hpos1.data(), contig ? pos2 : hpos2.data(), slot2orig,
-                          slot2pair, cand2pair, cand_list, ylm_n, w_n, coef_n, grid_n, 0, lap_total);
+                          slot2pair, cand2pair, cand_list, ylm_n, w_n, coef_n, grid_n, 0, lap_total,
+                          pl->tc_meta.size(), tc_s);
     if (s) { fo_plan_destroy(pl); return s; }
     pl->sb.dtab = pl->fp32 ? (const void *const *)ctx->d_dtab32 : (const void *const *)ctx->d_dtab64;
     *out = pl;
@@ -791,6 +918,29 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
     return FO_OK;
 }
 
+// After the stream has drained: the tensor-core contraction's timeout flag.
+static fo_status tc_status(fo_plan *pl) {
+    if (!pl->tc) return FO_OK;
+    int terr = 0;
+    fo_status s = cuda_check(pl->ctx, cudaMemcpy(&terr, pl->tcb.err, sizeof(int), cudaMemcpyDeviceToHost), "status");
+    if (s) return s;
+    return terr ? set_err(pl->ctx, FO_ERR_CUDA, "tensor-core Wigner contraction: a pipeline wait timed out") : FO_OK;
+}
+
+// The inverse SO(3) transform of a plan's coefficients onto its grids: the
+// tensor-core contraction and its FFT stage, or the fused CUDA-core kernel.
+static void launch_isoft_stage(fo_plan *pl, cudaStream_t st, bool events) {
+    if (pl->tc) {
+        cudaMemsetAsync(pl->tcb.err, 0, sizeof(int), st);
+        fo::launch_wigner_tc(pl->tcb, st);
+        if (events) rec_event(pl, K_WTC);
+        fo::launch_isoft_tc(pl->tcb, st);
+    } else {
+        fo::launch_isoft(pl->sb, pl->fp32, st);
+    }
+    if (events) rec_event(pl, K_ISOFT);
+}
+
 // The plan's launch sequence on the context's stream (the refinement buckets
 // fork onto the auxiliary streams and join back).  events: per-stage profile
 // events (not while a graph is captured).
@@ -810,7 +960,7 @@ static void plan_enqueue(fo_plan *pl, bool events) {
         fo::launch_sph_ylm(pl->sb, pl->fp32, st); rec_event(pl, K_YLM);
         fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st); rec_event(pl, K_RADIAL);
         fo::launch_sph_coeff(pl->sb, pl->fp32, st); rec_event(pl, K_COEFF);
-        fo::launch_isoft(pl->sb, pl->fp32, st);    rec_event(pl, K_ISOFT);
+        launch_isoft_stage(pl, st, events);
     } else {
         cudaMemsetAsync(pl->d_fgrid, 0, pl->fgrid_bytes, st);
         rec_event(pl, K_MEMSET);
@@ -867,6 +1017,8 @@ fo_status fo_plan_wait(fo_plan *pl) {
     if (!pl) return FO_ERR_BAD_ARGS;
     fo_ctx *ctx = pl->ctx;
     fo_status s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "pipeline");
+    if (s) return s;
+    s = tc_status(pl);
     if (s) return s;
     if (ctx->opts.profile && pl->evs.size() > 1) {
         for (size_t i = 1; i < pl->evs.size(); ++i) {
@@ -933,7 +1085,8 @@ int fo_plan_launches(const fo_plan *pl) {
     // cluster: centre, ylm, radial, coeff, isoft; bulk: prep, sf, 3 fft passes;
     // then findpeaks (5^3 window, wider windows), one refinement launch per
     // bucket, select
-    return (pl->bulk ? 5 : 5) + 2 + nb + 1;
+    const int tcl = pl->tc ? (int)pl->tcb.launches.size() + 1 : 0;   // contraction launches and the FFT stage
+    return (pl->bulk ? 5 : 5) + tcl + 2 + nb + 1;
 }
 
 void fo_plan_destroy(fo_plan *pl) {
@@ -1068,8 +1221,9 @@ fo_status fo_cluster_overlap(fo_ctx *ctx, const fo_cluster_pair *pair, const dou
     fo::launch_sph_ylm(pl->sb, pl->fp32, st);
     fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
     fo::launch_sph_coeff(pl->sb, pl->fp32, st);
-    fo::launch_isoft(pl->sb, pl->fp32, st);
+    launch_isoft_stage(pl, st, false);
     s = cuda_check(ctx, cudaStreamSynchronize(st), "cluster overlap");
+    if (!s) s = tc_status(pl);
     const int L = q.jmax, W = 2 * L + 1, G = 2 * (L + 1);
     const size_t ncoef = 2 * (size_t)(L + 1) * W * W, ngrid = (size_t)G * G * G;
     const size_t tsz = pl->fp32 ? 4 : 8;
@@ -1424,10 +1578,11 @@ fo_status fo_calc_overlap_matrices(fo_ctx *ctx, const double *coordslist, int na
         fo::launch_sph_ylm(pl->sb, pl->fp32, st);
         fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
         fo::launch_sph_coeff(pl->sb, pl->fp32, st);
-        fo::launch_isoft(pl->sb, pl->fp32, st);
+        launch_isoft_stage(pl, st, false);
         fo::launch_pair_stats(pl->sb, pl->fp32, d_out, st);
         cudaMemcpyAsync(h.data(), d_out, 2 * nb * sizeof(double), cudaMemcpyDeviceToHost, st);
         s = cuda_check(ctx, cudaStreamSynchronize(st), "overlap matrices");
+        if (!s) s = tc_status(pl);
         fo_plan_destroy(pl);
         for (size_t k = 0; k < nb && !s; ++k) {
             const int i1 = todo[c0 + k].first, i2 = todo[c0 + k].second;

@@ -199,6 +199,29 @@ __device__ T2 *fft_lines(T2 *x, T2 *y, int n, int nlines, int lstride, int estri
     return x;
 }
 
+// The transform tail of one beta index k of the inverse SO(3) transform (both
+// orientations): bufA / bufC hold the (m1, m2) sums of the direct and the
+// inverted orientation at ((m1 mod G) * G + (m2 mod G)); unnormalised
+// backward DFTs m2 -> gamma and m1 -> alpha in shared memory, then the real
+// part to grid_pair[o * G^3 + a + G * (k + G * g)] (alpha fastest).  bufB is
+// scratch; tw[t] = exp(+2 pi i t / G).  All threads of the block call it.
+template <typename T, typename T2>
+__device__ void isoft_tail(T2 *bufA, T2 *bufB, T2 *bufC, const T2 *tw, int G, int k, bool inv,
+                           T *grid_pair) {
+    for (int o = 0; o < (inv ? 2 : 1); ++o) {
+        T2 *src = o ? bufC : bufA, *scr = bufB;
+        T2 *r1 = fft_lines(src, scr, G, G, G, 1, +1, tw);       // m2 -> gamma
+        T2 *o1 = (r1 == src) ? scr : src;
+        T2 *r2 = fft_lines(r1, o1, G, G, 1, G, +1, tw);         // m1 -> alpha
+        T *out = grid_pair + (long long)o * G * G * G + (long long)G * k;
+        for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+            const int a = t % G, g = t / G;
+            out[a + (long long)G * G * g] = r2[a * G + g].x;
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Euler matrix of EULERM (fastclusters.f90:990-1016), row-major.
 __host__ __device__ inline void euler_matrix(double a, double b, double g, double *R) {

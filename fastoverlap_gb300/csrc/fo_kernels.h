@@ -2,8 +2,10 @@
 // used by the C-ABI layer (fo_api.cu).  All launches are asynchronous on the
 // given stream.
 #pragma once
+#include <cuda.h>   // CUtensorMap (types only; the driver entry point is looked up at run time)
 #include <cuda_runtime.h>
 #include <mutex>
+#include <vector>
 #include "../../include/fastoverlap_gb300.h"
 #include "fo_common.cuh"
 
@@ -112,6 +114,49 @@ void launch_findpeaks_from(const PairDev *pairs, int npairs, void *grid, double 
 void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,
                    cudaEvent_t fork, cudaEvent_t *join);
 void launch_select(const RefineBuffers &b, cudaStream_t s);
+
+// tensor-core Wigner contraction (mixed form), fo_wigner_tc.cu
+constexpr int kTcTile = 64;        // pairs per tile: 128 MMA rows (real parts, then imaginary parts)
+constexpr int kTcMaxBuckets = 8;   // bandwidths (Wigner tables) per launch
+constexpr int kTcChunk = 64;       // (m1, m2) combinations per work item
+
+struct TcTile {
+    int L;            // Jmax of every pair of the tile
+    int bucket;       // index of its table in the launch's TcMaps
+    int npairs;       // pairs in the tile (<= kTcTile)
+    int pad;
+    long long s0;     // offset (floats) of the tile's sums in S: [col < 2G][row < 128][mm < W2p]
+    long long coef0[kTcTile];   // complex offset of each pair's coefficients (ilmm layout)
+};
+struct TcItem { int tile, mm0, mm1, pad; };
+struct TcPairMap { long long s0; int row, pad; };
+struct TcMaps {
+    CUtensorMap map[kTcMaxBuckets];   // Wigner tables [hi|lo][mm][Nr][32] (TMA, 128-byte swizzle)
+    int nr[kTcMaxBuckets];            // rows per mm: 2G rounded up to 16
+};
+struct TcLaunch {
+    TcMaps maps;
+    int item0, nitems, nrmax;
+};
+struct TcBuffers {
+    const PairDev *pairs = nullptr;
+    const TcTile *tiles = nullptr;
+    const TcItem *items = nullptr;
+    const TcPairMap *pmap = nullptr;
+    const void *coef = nullptr;   // complex FP32 coefficients
+    float *S = nullptr;           // contraction sums
+    void *grid = nullptr;         // FP32 overlap grids
+    int *err = nullptr;           // set when a wait timed out
+    int npairs = 0, maxG = 0;
+    std::vector<TcLaunch> launches;
+};
+int tc_rows(int bw);                 // Nr of a bandwidth
+size_t tc_table_floats(int bw);      // floats of its table
+// fills `out` (tc_table_floats(bw) floats) from the FP64 Wigner table and
+// encodes its tensor map; false when the tensor-map encoder is unavailable
+bool tc_make_table(int bw, const double *d64, float *out, CUtensorMap *map, cudaStream_t s);
+void launch_wigner_tc(const TcBuffers &b, cudaStream_t s);   // the contraction (tcgen05)
+void launch_isoft_tc(const TcBuffers &b, cudaStream_t s);    // the FFT stage after it
 
 // context options (library-internal; the server creates worker contexts)
 fo_opts ctx_opts(const fo_ctx *ctx);

@@ -502,18 +502,7 @@ __global__ void __launch_bounds__(256) k_isoft(const PairDev *pairs, const T2 *c
         bufC[dst] = pack2<T2, T>(er - orr, ei - oi);
     }
     __syncthreads();
-    for (int o = 0; o < (inv ? 2 : 1); ++o) {
-        T2 *src = o ? bufC : bufA, *scr = bufB;
-        T2 *r1 = fft_lines(src, scr, G, G, G, 1, +1, tw);       // m2 -> gamma
-        T2 *o1 = (r1 == src) ? scr : src;
-        T2 *r2 = fft_lines(r1, o1, G, G, 1, G, +1, tw);         // m1 -> alpha
-        T *out = grid + P.grid0 + (long long)o * G * G * G + (long long)G * k;
-        for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
-            const int a = t % G, g = t / G;
-            out[a + (long long)G * G * g] = r2[a * G + g].x;
-        }
-        __syncthreads();
-    }
+    isoft_tail<T, T2>(bufA, bufB, bufC, tw, G, k, inv, grid + P.grid0);
 }
 
 // ---------------------------------------------------------------------------

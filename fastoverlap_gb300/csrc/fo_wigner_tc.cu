@@ -1,0 +1,476 @@
+// fo_wigner_tc.cu -- the Wigner-d contraction of the inverse SO(3) transform
+// on the tcgen05 tensor cores (mixed form), and the FFT stage that follows it.
+//
+// Reference behaviour (matthewghgriffiths/fastoverlap): ISOFT
+// fastoverlap/f90/DSOFT.f90:265-329 (soft.py:115-125 in the Python path):
+//   T[m1, beta_k, m2] = sum_{l >= max(|m1|,|m2|)} d^l_{m1 m2}(beta_k) I^l_{m1 m2}
+// followed by inverse FFTs over m2 -> gamma and m1 -> alpha.
+//
+// GEMM form.  Pairs of one bandwidth are grouped into tiles of 64.  For each
+// (m1, m2) -- "mm", W^2 of them -- the contraction over l of all pairs of a
+// tile and all beta_k is one product
+//   D[row][col] = sum_l A[row][l] B[col][l]
+//     row < 128: real parts of the 64 pairs' I^l_{m1m2}, then imaginary parts
+//     col < 2G : beta_k of the direct orientation, then of the inverted one
+//                (B[G + k][l] = (-1)^l d^l(beta_k), since I_inv^l = (-1)^l I^l)
+//     l   < 32 : zero beyond the bandwidth
+// issued as tcgen05.mma kind::tf32 with M = 128, N = Nr (2G rounded up to 16),
+// K = 8 per instruction, the FP32 accumulator in tensor memory.  Precision is
+// FP32-like by 3xTF32 splitting: x = hi + lo with hi the operand rounded to
+// TF32, and D = A_hi B_hi + A_hi B_lo + A_lo B_hi (the dropped A_lo B_lo term
+// is ~2^-22 relative).
+//
+// Data movement.  B (the Wigner tables, split into hi/lo once per bandwidth
+// from the FP64 recurrence, layout [hi|lo][mm][Nr rows][32 l]) arrives by TMA
+// (cp.async.bulk.tensor, 128-byte swizzle) into shared memory.  A is read from
+// the coefficient array by four producer warps, split into hi/lo in registers
+// and written to shared memory in the same 128-byte-swizzled K-major layout.
+// A single thread issues the MMAs; four epilogue warps read the accumulators
+// (tcgen05.ld, warp w owns TMEM lanes 32w..32w+31) for four mm at a time and
+// write the sums to S[tile][col][row][mm] (mm fastest, 16-byte stores), where
+// the FFT kernel below reads each (pair, beta_k) as contiguous runs.
+//
+// Every wait on an mbarrier is bounded (about two seconds on the global
+// timer); a wait that runs out sets *err, the CTA leaves its loops, frees its
+// tensor memory and returns, and the host reports FO_ERR_CUDA.
+#include <cuda.h>   // CUtensorMap and the tensor-map enums (no driver library link)
+
+#include "fo_common.cuh"
+#include "fo_kernels.h"
+
+#include <mutex>
+
+namespace fo {
+
+namespace {
+
+constexpr int kTcStages = 2;
+constexpr int kTcThreads = 288;          // warps 0-3 epilogue, 4-7 A producers, 8 MMA
+constexpr int kTcBatch = 4;              // mm per accumulator group
+constexpr int kTcRowBytes = 128;         // 32 FP32 values of l per row
+constexpr int kTcABytes = 128 * kTcRowBytes;
+constexpr long long kTcWaitNs = 2000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase with the given parity to complete; false when the time
+// limit passes or another role of the CTA has given up (*abort).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    for (;;) {
+        if (mbar_try(bar, parity)) return true;
+        if (*abort) return false;
+        if ((long long)(gtimer() - t0) > kTcWaitNs) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte
+// swizzled layout (8 rows of 128 bytes per 1024-byte atom, atoms stacked
+// along M/N): start address >> 4 (bits 0-13), leading byte offset (unused by
+// swizzled K-major layouts, 16 B), stride byte offset 1024 >> 4 (bits
+// 32-45), descriptor version 1 (bit 46), swizzle mode 2 = 128 B (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
+// (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 in bits
+// 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t tf32_idesc(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+            d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ float tf32_round(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Wigner tables in the MMA layout, from the FP64 table d64 ([k][l][i1][i2],
+// k < G, l < bw): out[h][mm][row][l] (h = 0 hi, 1 lo; row < Nr; l < 32) with
+// row = o G + k (o = 1: times (-1)^l), zero for l >= bw and rows >= 2G.
+__global__ void k_wigner_tc_table(int bw, const double *__restrict__ d64, float *__restrict__ out, int Nr) {
+    const int W = 2 * bw - 1, W2 = W * W, G = 2 * bw;
+    const long long n = (long long)W2 * Nr * 32;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int l = (int)(t % 32), row = (int)((t / 32) % Nr), mm = (int)(t / (32LL * Nr));
+    double x = 0.0;
+    if (l < bw && row < 2 * G) {
+        const int o = row / G, k = row % G;
+        x = d64[((long long)k * bw + l) * W2 + mm];
+        if (o && (l & 1)) x = -x;
+    }
+    const float hi = tf32_round((float)x);
+    out[t] = hi;
+    out[n + t] = (float)(x - (double)hi);
+}
+
+// ---------------------------------------------------------------------------
+// The contraction.  One CTA per work item (a tile and a range of mm).
+__global__ void __launch_bounds__(kTcThreads, 2)
+    k_wigner_tc(const __grid_constant__ TcMaps maps, const TcTile *__restrict__ tiles,
+                const TcItem *__restrict__ items, const float2 *__restrict__ coef, float *__restrict__ S,
+                int tmem_cols, int nrmax, int *err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t bars[3 * kTcStages + 2];
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ int abort_sh;
+    __shared__ long long coef0_sh[kTcTile];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const TcItem it = items[blockIdx.x];
+    const TcTile &T = tiles[it.tile];
+    const int L = T.L, bw = L + 1, G = 2 * bw, W = 2 * L + 1, W2p = ((W * W + 3) / 4) * 4;
+    const int Nr = maps.nr[T.bucket], nks = (bw + 7) / 8, nmm = it.mm1 - it.mm0;
+    const int npairs = T.npairs;
+    const CUtensorMap *map = &maps.map[T.bucket];
+    const uint32_t idesc = tf32_idesc(128, Nr);
+
+    // 1024-aligned carve: A[stage][hi|lo] (16 KB each), B[stage][hi|lo] (nrmax x 128 B)
+    const uint32_t sbase = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    unsigned char *gbase = smem_raw + (sbase - smem_u32(smem_raw));
+    auto a_addr = [&](int s, int h) { return sbase + (uint32_t)((2 * s + h) * kTcABytes); };
+    const uint32_t bsz = (uint32_t)nrmax * kTcRowBytes;
+    auto b_addr = [&](int s, int h) { return sbase + 2u * kTcStages * kTcABytes + (uint32_t)(2 * s + h) * bsz; };
+    auto full_a = [&](int s) { return smem_u32(&bars[s]); };
+    auto full_b = [&](int s) { return smem_u32(&bars[kTcStages + s]); };
+    auto empty = [&](int s) { return smem_u32(&bars[2 * kTcStages + s]); };
+    const uint32_t acc_full = smem_u32(&bars[3 * kTcStages]), acc_empty = smem_u32(&bars[3 * kTcStages + 1]);
+
+    if (tid == 0) {
+        for (int s = 0; s < kTcStages; ++s) {
+            mbar_init(full_a(s), 128);
+            mbar_init(full_b(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, 128);
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int p = tid; p < kTcTile; p += kTcThreads) coef0_sh[p] = T.coef0[p];
+    if (warp == 8) {   // tensor memory: four accumulators of Nr columns
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                     "r"(tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = tmem_base_sh;
+    volatile int *abort = &abort_sh;
+    auto give_up = [&]() {
+        *abort = 1;
+        atomicOr(err, 1);
+    };
+
+    if (warp >= 4 && warp < 8) {
+        // ---- A producers: row r = pair (r & 63), real (r < 64) or imaginary part
+        const int r = tid - 128, p = r & 63, part = r >> 6;
+        const bool valid = p < npairs;
+        const float2 *cp = coef + (valid ? coef0_sh[p] : 0);
+        const int nchunk = 2 * nks;   // 16-byte chunks (4 values of l) the MMAs read
+        for (int j = 0; j < nmm; ++j) {
+            const int s = j % kTcStages;
+            if (j >= kTcStages && !mbar_wait(empty(s), ((j / kTcStages) - 1) & 1, abort)) { give_up(); break; }
+            const int mm = it.mm0 + j;
+            if (r == 0) {   // B by TMA: the hi and lo tables of this mm
+                mbar_expect_tx(full_b(s), 2u * (uint32_t)Nr * kTcRowBytes);
+                tma_load_2d(b_addr(s, 0), map, 0, mm * Nr, full_b(s));
+                tma_load_2d(b_addr(s, 1), map, 0, (W * W + mm) * Nr, full_b(s));
+            }
+            const int i1 = mm / W, i2 = mm % W;
+            float v[32];
+#pragma unroll
+            for (int l = 0; l < 32; ++l) {
+                v[l] = 0.f;
+                if (valid && l < bw) {
+                    const float2 c = cp[((long long)l * W + i1) * W + i2];
+                    v[l] = part ? c.y : c.x;
+                }
+            }
+            unsigned char *ah = gbase + (a_addr(s, 0) - sbase), *al = gbase + (a_addr(s, 1) - sbase);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                if (c < nchunk) {
+                    float4 h, lo;
+                    h.x = tf32_round(v[4 * c]);     lo.x = v[4 * c] - h.x;
+                    h.y = tf32_round(v[4 * c + 1]); lo.y = v[4 * c + 1] - h.y;
+                    h.z = tf32_round(v[4 * c + 2]); lo.z = v[4 * c + 2] - h.z;
+                    h.w = tf32_round(v[4 * c + 3]); lo.w = v[4 * c + 3] - h.w;
+                    const int off = r * kTcRowBytes + ((c ^ (r & 7)) << 4);
+                    *reinterpret_cast<float4 *>(ah + off) = h;
+                    *reinterpret_cast<float4 *>(al + off) = lo;
+                }
+            }
+            fence_async_smem();   // generic-proxy stores -> visible to the tensor cores
+            mbar_arrive(full_a(s));
+        }
+    } else if (warp == 8) {
+        // ---- MMA issuer (one thread)
+        if (lane == 0) {
+            for (int j = 0; j < nmm; ++j) {
+                const int s = j % kTcStages, slot = j % kTcBatch, q = j / kTcBatch;
+                if (slot == 0 && q > 0) {
+                    if (!mbar_wait(acc_empty, (q - 1) & 1, abort)) { give_up(); break; }
+                }
+                const uint32_t ph = (j / kTcStages) & 1;
+                if (!mbar_wait(full_a(s), ph, abort) || !mbar_wait(full_b(s), ph, abort)) { give_up(); break; }
+                tc_fence_after();
+                const uint32_t d = tbase + (uint32_t)(slot * Nr);
+                for (int ks = 0; ks < nks; ++ks) {
+                    const uint64_t ah = sw128_desc(a_addr(s, 0) + 32u * ks), alo = sw128_desc(a_addr(s, 1) + 32u * ks);
+                    const uint64_t bh = sw128_desc(b_addr(s, 0) + 32u * ks), blo = sw128_desc(b_addr(s, 1) + 32u * ks);
+                    mma_tf32(d, ah, bh, idesc, ks > 0 ? 1u : 0u);
+                    mma_tf32(d, ah, blo, idesc, 1u);
+                    mma_tf32(d, alo, bh, idesc, 1u);
+                }
+                mma_commit(empty(s));
+                if (slot == kTcBatch - 1 || j == nmm - 1) mma_commit(acc_full);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31 (rows)
+        const int row = 32 * warp + lane, p = row & 63;
+        const bool valid = p < npairs;
+        const uint32_t lrow = tbase + ((uint32_t)(32 * warp) << 16);
+        const int ncol = 2 * G;
+        const long long ldm = W2p;
+        float *base = S + T.s0 + (long long)row * ldm;
+        const int nbatch = (nmm + kTcBatch - 1) / kTcBatch;
+        for (int q = 0; q < nbatch; ++q) {
+            if (!mbar_wait(acc_full, q & 1, abort)) { give_up(); break; }
+            tc_fence_after();
+            const int nb = min(kTcBatch, nmm - kTcBatch * q), mmq = it.mm0 + kTcBatch * q;
+            for (int cc = 0; cc < ncol; cc += 16) {
+                uint32_t v0[16], v1[16], v2[16], v3[16];
+                tmem_ld16(lrow + (uint32_t)(0 * Nr + cc), v0);
+                tmem_ld16(lrow + (uint32_t)(1 * Nr + cc), v1);
+                tmem_ld16(lrow + (uint32_t)(2 * Nr + cc), v2);
+                tmem_ld16(lrow + (uint32_t)(3 * Nr + cc), v3);
+                tmem_ld_wait();
+                if (valid) {
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        const int col = cc + c;
+                        if (col < ncol) {
+                            float *dst = base + (long long)col * 128 * ldm + mmq;
+                            if (nb == 4) {
+                                *reinterpret_cast<float4 *>(dst) =
+                                    make_float4(__uint_as_float(v0[c]), __uint_as_float(v1[c]), __uint_as_float(v2[c]),
+                                                __uint_as_float(v3[c]));
+                            } else {
+                                dst[0] = __uint_as_float(v0[c]);
+                                if (nb > 1) dst[1] = __uint_as_float(v1[c]);
+                                if (nb > 2) dst[2] = __uint_as_float(v2[c]);
+                            }
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(acc_empty);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 8) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(tmem_cols) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FFT stage: one block per (beta index k, pair), both orientations: the
+// contraction's sums of the pair's row are contiguous in mm; scattered into
+// the (m1, m2) grid, then the transform tail shared with k_isoft.
+__global__ void __launch_bounds__(256) k_isoft_tc(const PairDev *pairs, const TcPairMap *pmap, const float *S,
+                                                  float *grid) {
+    extern __shared__ __align__(16) unsigned char smem_fft[];
+    const int k = blockIdx.x, p = blockIdx.y;
+    const PairDev P = pairs[p];
+    const int G = P.G, L = P.L, Wc = 2 * L + 1, W2 = Wc * Wc, W2p = ((W2 + 3) / 4) * 4;
+    if (k >= G) return;
+    const bool inv = P.norient == 2;
+    float2 *bufA = (float2 *)smem_fft, *bufB = bufA + G * G, *bufC = bufB + G * G, *tw = bufC + G * G;
+    for (int t = threadIdx.x; t < G; t += blockDim.x) {
+        float sn, cs;
+        sincospif(2.0f * t / G, &sn, &cs);
+        tw[t] = make_float2(cs, sn);
+    }
+    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+        bufA[t] = make_float2(0.f, 0.f);
+        bufC[t] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const TcPairMap pm = pmap[p];
+    const float *re0 = S + pm.s0 + ((long long)k * 128 + pm.row) * W2p;
+    const float *im0 = re0 + 64LL * W2p;
+    const float *re1 = re0 + (long long)G * 128 * W2p, *im1 = re1 + 64LL * W2p;
+    for (int t = threadIdx.x; t < W2; t += blockDim.x) {
+        const int i1 = t / Wc, i2 = t % Wc;
+        const int m1 = (i1 <= L) ? i1 : i1 - Wc, m2 = (i2 <= L) ? i2 : i2 - Wc;
+        const int dst = ((m1 + G) % G) * G + (m2 + G) % G;
+        bufA[dst] = make_float2(re0[t], im0[t]);
+        if (inv) bufC[dst] = make_float2(re1[t], im1[t]);
+    }
+    __syncthreads();
+    isoft_tail<float, float2>(bufA, bufB, bufC, tw, G, k, inv, grid + P.grid0);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    });
+    return fn;
+}
+
+int pow2_at_least(int x) {
+    int p = 32;
+    while (p < x) p *= 2;
+    return p;
+}
+
+// Dynamic shared memory of one CTA and its tensor-memory columns; the shared
+// memory is raised when needed so that the CTAs resident on an SM never ask
+// for more than the 512 columns there are.
+void tc_footprint(int nrmax, size_t *smem, int *cols) {
+    *cols = pow2_at_least(kTcBatch * nrmax);
+    size_t sm = 1024 + 2ull * kTcStages * kTcABytes + 2ull * kTcStages * nrmax * kTcRowBytes;
+    const size_t per_sm = 228 * 1024, reserved = 1024 + 4096;   // per-CTA reservation and static smem
+    while ((int)(per_sm / (sm + reserved)) * (*cols) > 512) sm += 8 * 1024;
+    *smem = sm;
+}
+
+}  // namespace
+
+int tc_rows(int bw) { return ((4 * bw + 15) / 16) * 16; }
+
+size_t tc_table_floats(int bw) {
+    const int W = 2 * bw - 1;
+    return 2ull * W * W * tc_rows(bw) * 32;
+}
+
+bool tc_make_table(int bw, const double *d64, float *out, CUtensorMap *map, cudaStream_t s) {
+    const int Nr = tc_rows(bw), W = 2 * bw - 1;
+    const long long n = (long long)W * W * Nr * 32;
+    k_wigner_tc_table<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(bw, d64, out, Nr);
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {32, (cuuint64_t)2 * W * W * Nr};
+    const cuuint64_t strides[1] = {32 * sizeof(float)};
+    const cuuint32_t box[2] = {32, (cuuint32_t)Nr};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, out, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+void launch_wigner_tc(const TcBuffers &b, cudaStream_t s) {
+    allow_max_smem<k_wigner_tc>();
+    for (const TcLaunch &lg : b.launches) {
+        size_t sm;
+        int cols;
+        tc_footprint(lg.nrmax, &sm, &cols);
+        k_wigner_tc<<<lg.nitems, kTcThreads, sm, s>>>(lg.maps, b.tiles, b.items + lg.item0, (const float2 *)b.coef,
+                                                       b.S, cols, lg.nrmax, b.err);
+    }
+}
+
+void launch_isoft_tc(const TcBuffers &b, cudaStream_t s) {
+    const size_t fsm = sizeof(float2) * (3 * b.maxG * b.maxG + b.maxG);
+    allow_max_smem<k_isoft_tc>();
+    k_isoft_tc<<<dim3(b.maxG, b.npairs), 256, fsm, s>>>(b.pairs, b.pmap, b.S, (float *)b.grid);
+}
+
+}  // namespace fo

@@ -123,6 +123,11 @@ void        fo_ctx_destroy(fo_ctx *ctx);
 const char *fo_status_string(fo_status s);
 const char *fo_last_error(const fo_ctx *ctx);
 fo_status   fo_set_precision(fo_ctx *ctx, int precision);
+/* Mixed form: 1 (default) runs the Wigner-d contraction of the inverse SO(3)
+ * transform (ISOFT, fastoverlap/f90/DSOFT.f90:286-299) on the tcgen05 tensor
+ * cores in split TF32 (3xTF32, FP32 accumulation); 0 on the FP32 CUDA cores.
+ * Applies to plans created afterwards; the FP64 form never uses it.          */
+fo_status   fo_set_tensor_cores(fo_ctx *ctx, int on);
 
 /* ---- batched entry points (host buffers in, host buffers out) ----
  * pos1 = target structures (COORDSB), pos2 = structures moved onto them
