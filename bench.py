@@ -268,23 +268,30 @@ def allmax(dist, v):
     return float(t.item())
 
 
-def cpu_baseline_run(pairs, nthreads, budget_s=20.0):
-    """Oracle (CPU restatement of the reference algorithm) on a bounded sample."""
+def _oracle_sample(pairs, nthreads, budget_s, per_call=None):
+    """The oracle (CPU restatement of the reference algorithm) over a bounded
+    sample of the workload, in calls of per_call pairs (default 8 per thread,
+    so that the threads' dynamic pair queue stays balanced), until budget_s
+    of CPU time has passed.  Returns (pairs/s, pairs done, seconds, per_call)."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import oracle as O
     sample = [dict(pos1=p[0], pos2=p[1], perm=p[2], Jmax=p[3], sigma=0.3) for p in pairs]
-    n = min(len(sample), max(nthreads, 8))
-    t0 = time.time()
-    O.cluster_align_many(sample[:n], nrot=10, invert=True, cutoff=True, nthreads=nthreads)
-    dt = time.time() - t0
-    done = n
-    while dt < budget_s * 0.5 and done + n <= len(sample):
-        t1 = time.time()
-        O.cluster_align_many(sample[done:done + n], nrot=10, invert=True, cutoff=True,
-                             nthreads=nthreads)
-        dt += time.time() - t1
-        done += n
-    return done / dt, done, dt
+    per_call = per_call or 8 * nthreads
+    done, dt = 0, 0.0
+    while dt < budget_s:
+        chunk = [sample[(done + i) % len(sample)] for i in range(per_call)]
+        t0 = time.time()
+        O.cluster_align_many(chunk, nrot=10, invert=True, cutoff=True, nthreads=nthreads)
+        dt += time.time() - t0
+        done += per_call
+    return done / dt, done, dt, per_call
+
+
+def cpu_baseline_run(pairs, nthreads, budget_s=10.0):
+    """CPU baseline of the oracle port beside the GPU line (same sampler as
+    the reference arm)."""
+    v, done, dt, _ = _oracle_sample(pairs, nthreads, budget_s)
+    return v, done, dt
 
 
 def run_reference(args, pairs):
@@ -296,17 +303,15 @@ def run_reference(args, pairs):
     import oracle as O
     O.build()
     sample = [dict(pos1=p[0], pos2=p[1], perm=p[2], Jmax=p[3], sigma=0.3) for p in pairs]
-    per_step = max(nthreads * 2, 16)
     for w in range(args.warmup):
         O.cluster_align_many(sample[:nthreads], nthreads=nthreads)
+    # each step: one call of 8 pairs per thread (the same sampler as the
+    # in-arm baseline), walking through the workload
     times = []
-    done = 0
+    per_step = 8 * nthreads
     for s in range(args.steps):
-        chunk = [sample[(done + i) % len(sample)] for i in range(per_step)]
-        t0 = time.time()
-        O.cluster_align_many(chunk, nthreads=nthreads)
-        times.append(time.time() - t0)
-        done += per_step
+        v, done, dt, _ = _oracle_sample(pairs[(s * per_step) % len(pairs):] + pairs, nthreads, 0.0, per_step)
+        times.append(dt)
     tot = sum(times)
     val = per_step * args.steps / tot
     line = {"metric": METRIC, "value": val, "unit": "pairs/s", "n_gpus": args.gpus,

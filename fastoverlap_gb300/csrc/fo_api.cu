@@ -621,9 +621,9 @@ static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
             T.s0 = (long long)sfl;
             for (int i = 0; i < T.npairs; ++i) {
                 T.coef0[i] = pl->hp[order[t0 + i]].coef0;
-                pmap[order[t0 + i]] = fo::TcPairMap{(long long)sfl, i, 0};
+                pmap[order[t0 + i]] = fo::TcPairMap{(long long)sfl, i, T.npairs};
             }
-            sfl += 2ull * G * 128 * W2p;
+            sfl += 2ull * G * 2 * T.npairs * W2p;
             tiles.push_back(T);
             tile_L.push_back(L);
         }

