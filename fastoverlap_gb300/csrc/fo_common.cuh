@@ -199,27 +199,51 @@ __device__ T2 *fft_lines(T2 *x, T2 *y, int n, int nlines, int lstride, int estri
     return x;
 }
 
+// Shared-memory (m1, m2) planes of the inverse SO(3) transform: G rows of
+// G + 1 elements (the pad keeps column walks free of bank conflicts).
+__host__ __device__ inline int isoft_ld(int G) { return G + 1; }
+__host__ __device__ inline int isoft_plane(int G) { return G * (G + 1); }
+
 // The transform tail of one beta index k of the inverse SO(3) transform (both
 // orientations): bufA / bufC hold the (m1, m2) sums of the direct and the
-// inverted orientation at ((m1 mod G) * G + (m2 mod G)); unnormalised
-// backward DFTs m2 -> gamma and m1 -> alpha in shared memory, then the real
-// part to grid_pair[o * G^3 + a + G * (k + G * g)] (alpha fastest).  bufB is
-// scratch; tw[t] = exp(+2 pi i t / G).  All threads of the block call it.
+// inverted orientation at ((m1 mod G) * ld + (m2 mod G)), ld = G + 1; the
+// unnormalised backward 2-D DFT (m2 -> gamma, m1 -> alpha) in shared memory,
+// then the real part to grid_pair[o * G^3 + a + G * (k + G * g)] (alpha
+// fastest).  Only real parts are kept, and Re F(X) = F(H(X)) with H(X)[m] =
+// (X[m] + conj X[-m]) / 2 (H(X) transforms to a real grid), so both
+// orientations go through ONE complex transform of Z = H(A) + i H(C): its
+// real part is the direct grid, its imaginary part the inverted one.  bufB
+// is scratch; tw[t] = exp(+2 pi i t / G).  All threads of the block call it.
 template <typename T, typename T2>
 __device__ void isoft_tail(T2 *bufA, T2 *bufB, T2 *bufC, const T2 *tw, int G, int k, bool inv,
                            T *grid_pair) {
-    for (int o = 0; o < (inv ? 2 : 1); ++o) {
-        T2 *src = o ? bufC : bufA, *scr = bufB;
-        T2 *r1 = fft_lines(src, scr, G, G, G, 1, +1, tw);       // m2 -> gamma
-        T2 *o1 = (r1 == src) ? scr : src;
-        T2 *r2 = fft_lines(r1, o1, G, G, 1, G, +1, tw);         // m1 -> alpha
-        T *out = grid_pair + (long long)o * G * G * G + (long long)G * k;
+    const int ld = isoft_ld(G);
+    T2 *src = bufA, *scr = bufB;
+    if (inv) {
         for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
-            const int a = t % G, g = t / G;
-            out[a + (long long)G * G * g] = r2[a * G + g].x;
+            const int i1 = t / G, i2 = t % G;
+            const int e = i1 * ld + i2, em = ((G - i1) % G) * ld + (G - i2) % G;
+            const T2 a = bufA[e], am = bufA[em], c = bufC[e], cm = bufC[em];
+            T2 z;
+            z.x = T(0.5) * ((a.x + am.x) - (c.y - cm.y));
+            z.y = T(0.5) * ((a.y - am.y) + (c.x + cm.x));
+            bufB[e] = z;
         }
         __syncthreads();
+        src = bufB;
+        scr = bufA;
     }
+    T2 *r1 = fft_lines(src, scr, G, G, ld, 1, +1, tw);      // m2 -> gamma
+    T2 *o1 = (r1 == src) ? scr : src;
+    T2 *r2 = fft_lines(r1, o1, G, G, 1, ld, +1, tw);        // m1 -> alpha
+    T *out0 = grid_pair + (long long)G * k, *out1 = out0 + (long long)G * G * G;
+    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+        const int a = t % G, g = t / G;
+        const T2 v = r2[a * ld + g];
+        out0[a + (long long)G * G * g] = v.x;
+        if (inv) out1[a + (long long)G * G * g] = v.y;
+    }
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------

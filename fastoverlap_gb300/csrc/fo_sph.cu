@@ -466,14 +466,15 @@ __global__ void __launch_bounds__(256) k_isoft(const PairDev *pairs, const T2 *c
     const int G = P.G, L = P.L, bw = L + 1, Wc = 2 * L + 1, W2 = Wc * Wc;
     if (k >= G) return;
     const bool inv = P.norient == 2;
-    T2 *bufA = (T2 *)smem_raw, *bufB = bufA + G * G, *bufC = bufB + G * G, *tw = bufC + G * G;
+    const int PL = isoft_plane(G), ld = isoft_ld(G);
+    T2 *bufA = (T2 *)smem_raw, *bufB = bufA + PL, *bufC = bufB + PL, *tw = bufC + PL;
     for (int t = threadIdx.x; t < G; t += blockDim.x) {
         T sn, cs;
         if constexpr (sizeof(T) == 4) sincospif(2.0f * t / G, &sn, &cs);
         else sincospi(2.0 * t / G, &sn, &cs);
         tw[t] = pack2<T2, T>(cs, sn);
     }
-    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+    for (int t = threadIdx.x; t < PL; t += blockDim.x) {
         bufA[t] = pack2<T2, T>(0, 0);
         bufC[t] = pack2<T2, T>(0, 0);
     }
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(256) k_isoft(const PairDev *pairs, const T2 *c
             orr += dv * c.x;
             oi += dv * c.y;
         }
-        const int dst = ((m1 + G) % G) * G + (m2 + G) % G;
+        const int dst = ((m1 + G) % G) * ld + (m2 + G) % G;
         bufA[dst] = pack2<T2, T>(er + orr, ei + oi);
         bufC[dst] = pack2<T2, T>(er - orr, ei - oi);
     }
@@ -602,12 +603,12 @@ void launch_pair_stats(const SphBuffers &b, bool fp32, double *out, cudaStream_t
 void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s) {
     dim3 grid(b.maxG, b.npairs);
     if (fp32) {
-        size_t sm = sizeof(float2) * (3 * b.maxG * b.maxG + b.maxG);
+        size_t sm = sizeof(float2) * (3 * isoft_plane(b.maxG) + b.maxG);
         allow_max_smem<k_isoft<float, float2>>();
         k_isoft<float, float2><<<grid, 256, sm, s>>>(b.pairs, (const float2 *)b.coef,
                                                     (const float *const *)b.dtab, (float *)b.grid);
     } else {
-        size_t sm = sizeof(double2) * (3 * b.maxG * b.maxG + b.maxG);
+        size_t sm = sizeof(double2) * (3 * isoft_plane(b.maxG) + b.maxG);
         allow_max_smem<k_isoft<double, double2>>();
         k_isoft<double, double2><<<grid, 256, sm, s>>>(b.pairs, (const double2 *)b.coef,
                                                       (const double *const *)b.dtab, (double *)b.grid);

@@ -368,13 +368,14 @@ __global__ void __launch_bounds__(256) k_isoft_tc(const PairDev *pairs, const Tc
     const int G = P.G, L = P.L, Wc = 2 * L + 1, W2 = Wc * Wc, W2p = ((W2 + 3) / 4) * 4;
     if (k >= G) return;
     const bool inv = P.norient == 2;
-    float2 *bufA = (float2 *)smem_fft, *bufB = bufA + G * G, *bufC = bufB + G * G, *tw = bufC + G * G;
+    const int PL = isoft_plane(G), ld = isoft_ld(G);
+    float2 *bufA = (float2 *)smem_fft, *bufB = bufA + PL, *bufC = bufB + PL, *tw = bufC + PL;
     for (int t = threadIdx.x; t < G; t += blockDim.x) {
         float sn, cs;
         sincospif(2.0f * t / G, &sn, &cs);
         tw[t] = make_float2(cs, sn);
     }
-    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+    for (int t = threadIdx.x; t < PL; t += blockDim.x) {
         bufA[t] = make_float2(0.f, 0.f);
         bufC[t] = make_float2(0.f, 0.f);
     }
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(256) k_isoft_tc(const PairDev *pairs, const Tc
     for (int t = threadIdx.x; t < W2; t += blockDim.x) {
         const int i1 = t / Wc, i2 = t % Wc;
         const int m1 = (i1 <= L) ? i1 : i1 - Wc, m2 = (i2 <= L) ? i2 : i2 - Wc;
-        const int dst = ((m1 + G) % G) * G + (m2 + G) % G;
+        const int dst = ((m1 + G) % G) * ld + (m2 + G) % G;
         bufA[dst] = make_float2(re0[t], im0[t]);
         if (inv) bufC[dst] = make_float2(re1[t], im1[t]);
     }
@@ -471,7 +472,7 @@ void launch_wigner_tc(const TcBuffers &b, cudaStream_t s) {
 }
 
 void launch_isoft_tc(const TcBuffers &b, cudaStream_t s) {
-    const size_t fsm = sizeof(float2) * (3 * b.maxG * b.maxG + b.maxG);
+    const size_t fsm = sizeof(float2) * (3 * isoft_plane(b.maxG) + b.maxG);
     allow_max_smem<k_isoft_tc>();
     k_isoft_tc<<<dim3(b.maxG, b.npairs), 256, fsm, s>>>(b.pairs, b.pmap, b.S, (float *)b.grid);
 }
