@@ -249,12 +249,14 @@ fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
     return FO_OK;
 }
 
-constexpr size_t kRefSmemCap = 96 * 1024;   // assignment arrays kept on chip up to this size
+constexpr size_t kRefSmemCap = 96 * 1024;     // assignment arrays kept on chip up to this size
+constexpr size_t kRefSplitCap = 120 * 1024;   // above it: only the working arrays on chip, up to this
 
 struct RefAssign {
     size_t smem;
     long long lapstride;
     int ct64;
+    int split;   // working arrays on chip, costs / neighbour lists in global scratch
 };
 
 // Shared-memory footprint of one refinement warp for a pair, and whether its
@@ -278,9 +280,17 @@ RefAssign ref_assign(int n, int maxg, bool fp32, bool recomp, double dmax) {
         }
         return (b + 127) & ~(size_t)127;
     };
+    r.split = 0;
     if (L.coord_end + L.lap_end <= kRefSmemCap) {
         r.smem = up(L.coord_end + L.lap_end);
         r.lapstride = 0;
+    } else if (L.coord_end + L.lap_small <= kRefSplitCap) {
+        // the assignment's random-access arrays and the neighbour-selection
+        // scratch stay on chip; the row-major neighbour lists (read a row at
+        // a time) go to the candidate's global scratch
+        r.smem = up(L.coord_end + L.lap_small);
+        r.lapstride = (long long)((L.lap_end + 255) & ~(size_t)255);
+        r.split = 1;
     } else {
         r.smem = up(L.coord_end);
         r.lapstride = (long long)((L.lap_end + 255) & ~(size_t)255);
@@ -745,6 +755,7 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
             double dmax = centred_radius(pos1 + 3 * q.coord_off, n) + centred_radius(pos2 + 3 * q.coord_off, n);
             RefAssign ra = ref_assign(n, maxg, pl->fp32, pl->fp32, dmax);
             P.lapstride = ra.lapstride;
+            P.lapsplit = ra.split;
             P.lap0 = lap_total;
             lap_total += (long long)P.norient * P.nrot * P.lapstride;
             rassign.push_back(ra);
@@ -882,6 +893,7 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
             double dmax = 0.5 * std::sqrt(q.box[0] * q.box[0] + q.box[1] * q.box[1] + q.box[2] * q.box[2]);
             RefAssign ra = ref_assign(n, maxg, pl->fp32, pl->fp32, dmax);
             P.lapstride = ra.lapstride;
+            P.lapsplit = ra.split;
             P.lap0 = lap_total;
             lap_total += (long long)P.nrot * P.lapstride;
             rassign.push_back(ra);

@@ -38,6 +38,8 @@ struct PairDev {
     int harm;         // cluster: 1 for the harmonic-oscillator basis (coordinates as given)
     int harm_n;       // its largest order nmax
     double harm_r0;   // its length scale (HWIDTH)
+    int lapsplit;     // 1: assignment working arrays on chip, costs / neighbour lists in the LAP scratch
+    int pad_;
 };
 
 struct GroupDev {

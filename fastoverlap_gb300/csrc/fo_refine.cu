@@ -932,12 +932,12 @@ struct GroupCoords {
 // Neighbour lists / costs of one group, then its assignment (PAIRDISTS +
 // JOVOSAP for one group).  Returns the assignment's status.
 template <typename KT, typename DT, typename CT, bool RECOMP, bool BOX>
-__device__ int assign_group(const int ns, const int m, const GroupCoords &G, unsigned char *lb,
+__device__ int assign_group(const int ns, const int m, const GroupCoords &G, unsigned char *lb, unsigned char *lbk,
                             const RefLayout &L) {
     const int lane = threadIdx.x & 31;
     const bool dense = (m == ns);
     constexpr bool kF32 = sizeof(DT) == 4;   // mixed form: no augmenting row reduction
-    KT *kk = (KT *)(lb + L.lap_kk);
+    KT *kk = (KT *)(lbk + L.lap_kk);
     long long *v = (long long *)(lb + L.lap_v), *dd = (long long *)(lb + L.lap_d);
     int *x = (int *)(lb + L.lap_x), *y = (int *)(lb + L.lap_y), *lab = (int *)(lb + L.lap_lab);
     int *fr = (int *)(lb + L.lap_fr), *todo = (int *)(lb + L.lap_todo);
@@ -960,7 +960,7 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
         };
         return run(CostF32<CT, BOX>{G.B4, G.A4, {G.bxf[0], G.bxf[1], G.bxf[2]}, {G.rxf[0], G.rxf[1], G.rxf[2]}});
     } else {
-        CT *cc = (CT *)(lb + L.lap_cc);
+        CT *cc = (CT *)(lbk + L.lap_cc);
         // squared distance of row i (bi: its FP64 coordinates) and column j
         auto dist = [&](int i, const double *bi, int j) -> DT {
             if constexpr (kF32)
@@ -1043,7 +1043,10 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     ref_layout(n, maxg, kF32, (int)sizeof(CT), RECOMP, L);
     float4 *B4 = (float4 *)(smem + L.DBf), *A4 = (float4 *)(smem + L.DAf);   // mixed form only
     int *permbest = (int *)(smem + L.perm), *newperm = (int *)(smem + L.nperm), *ptmp = (int *)(smem + L.ptmp);
-    unsigned char *lb = P.lapstride ? lapg + P.lap0 + (long long)local * P.lapstride : smem + L.coord_end;
+    // assignment block: on chip; or split (working arrays on chip, costs and
+    // neighbour lists in the candidate's global scratch); or all in global
+    unsigned char *lbk = P.lapstride ? lapg + P.lap0 + (long long)local * P.lapstride : smem + L.coord_end;
+    unsigned char *lb = (P.lapstride && !P.lapsplit) ? lbk : smem + L.coord_end;
     int *lx = (int *)(lb + L.lap_x);
     const double box[3] = {P.box[0], P.box[1], P.box[2]};
     const double *pk = peaks + 3LL * (P.cand0 + o * P.nrot + ci);
@@ -1188,8 +1191,8 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
                 GC.A = DA + 3 * s0;
                 GC.B4 = B4 + s0;
                 GC.A4 = A4 + s0;
-                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L)
-                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L);
+                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L)
+                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L);
                 if (rc) fail += 1;
                 __syncwarp();
                 for (int i = lane; i < ns; i += 32) {
@@ -1394,8 +1397,8 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
                 GC.A = DA + 3 * s0;
                 GC.B4 = B4 + s0;
                 GC.A4 = A4 + s0;
-                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L)
-                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, L);
+                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L)
+                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L);
                 if (rc) fail += 1;
                 __syncwarp();
                 for (int i = lane; i < ns; i += 32) {

@@ -8,6 +8,7 @@ namespace fo {
 struct RefLayout {
     size_t DBf, DAf, perm, nperm, ptmp, coord_end;
     size_t lap_cc, lap_kk, lap_heap, lap_v, lap_d, lap_x, lap_y, lap_lab, lap_fr, lap_todo, lap_ok, lap_end;
+    size_t lap_small;   // bytes of the assignment block before the costs and neighbour lists
     int kkbytes;   // bytes per neighbour-list column index
 };
 
@@ -42,9 +43,9 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     const int m = maxg < 60 ? maxg : 60;
     const bool sparse = maxg > 60;
     L.kkbytes = ref_kkbytes(maxg);
+    // the assignment's working arrays first, then the stored costs and the
+    // neighbour lists (the large part, which may live apart from the rest)
     size_t p = 0;
-    L.lap_cc = p; p += recomp ? 0 : ref_a16((size_t)ctsize * maxg * m);
-    L.lap_kk = p; p += sparse ? ref_a16((size_t)L.kkbytes * maxg * m) : 0;
     L.lap_v = p; p += ref_a16(8 * (size_t)maxg);
     L.lap_d = p; p += ref_a16(8 * (size_t)maxg);
     L.lap_x = p; p += ref_a16(4 * (size_t)maxg);
@@ -54,15 +55,20 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     L.lap_todo = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_ok = p; p += ref_a16((size_t)maxg);
     // the neighbour-selection scratch is only used before a group's
-    // assignment starts, so it overlays the assignment arrays
+    // assignment starts, so it overlays the working arrays (and never the
+    // neighbour lists it is filling)
     L.lap_heap = L.lap_v;
     size_t scratch = 0;
     if (recomp && sparse) {
         const size_t heap = 4 * 32 * (size_t)kHeapStride, row = 4 * (size_t)maxg;
         scratch = ref_a16(heap > row ? heap : row);   // groups up to maxg use either
     }
-    const size_t heap_end = L.lap_v + scratch;
-    L.lap_end = p > heap_end ? p : heap_end;
+    const size_t heap_end = L.lap_heap + scratch;
+    if (heap_end > p) p = heap_end;
+    L.lap_small = p;
+    L.lap_cc = p; p += recomp ? 0 : ref_a16((size_t)ctsize * maxg * m);
+    L.lap_kk = p; p += sparse ? ref_a16((size_t)L.kkbytes * maxg * m) : 0;
+    L.lap_end = p;
 }
 
 }  // namespace fo
