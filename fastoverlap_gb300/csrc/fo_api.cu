@@ -100,7 +100,7 @@ struct fo_plan {
     bool tc = false;         // Wigner contraction on the tensor cores
     fo::TcBuffers tcb;
     std::vector<unsigned char> tc_meta;         // tiles, items, pair map (host copy, uploaded once)
-    size_t tc_off_items = 0, tc_off_pmap = 0;   // their offsets in tc_meta (tiles at 0)
+    size_t tc_off_items = 0, tc_off_groups = 0;   // their offsets in tc_meta (tiles at 0)
 };
 
 namespace {
@@ -577,7 +577,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
         unsigned char *mb = (unsigned char *)P(o_tcm);
         t.tiles = (const fo::TcTile *)mb;
         t.items = (const fo::TcItem *)(mb + pl->tc_off_items);
-        t.pmap = (const fo::TcPairMap *)(mb + pl->tc_off_pmap);
+        t.groups = (const fo::TcFftGroup *)(mb + pl->tc_off_groups);
         t.pairs = pl->sb.pairs;
         t.coef = pl->sb.coef;
         t.grid = pl->sb.grid;
@@ -606,9 +606,9 @@ static bool packed_in_order(const PairT *pairs, int npairs) {
 
 // Tiles of the tensor-core contraction: the plan's pairs sorted by Jmax
 // (stable), 64 per tile; work items of kTcChunk (m1, m2) combinations; launch
-// groups of at most kTcMaxBuckets bandwidths.  Fills pl->tc_meta (tiles,
-// items, pair map) and pl->tcb.launches and returns the floats of the sum
-// buffer S.
+// groups of at most kTcMaxBuckets bandwidths; the FFT stage's groups of
+// pairs.  Fills pl->tc_meta (tiles, items, FFT groups) and pl->tcb and
+// returns the floats of the sum buffer S.
 static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
     const int np = pl->npairs;
     std::vector<int> order(np);
@@ -616,24 +616,34 @@ static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pl->hp[a].L < pl->hp[b].L; });
     std::vector<fo::TcTile> tiles;
     std::vector<fo::TcItem> items;
-    std::vector<fo::TcPairMap> pmap(np);
+    std::vector<fo::TcFftGroup> fgroups;
+    size_t fsm = 0;
     std::vector<int> tile_L;
     size_t sfl = 0;
     for (int a = 0; a < np;) {
         const int L = pl->hp[order[a]].L;
         int b = a;
         while (b < np && pl->hp[order[b]].L == L) ++b;
-        const int G = 2 * (L + 1), W2 = (2 * L + 1) * (2 * L + 1), W2p = ((W2 + 3) / 4) * 4;
+        const int G = 2 * (L + 1), W2 = (2 * L + 1) * (2 * L + 1);
         for (int t0 = a; t0 < b; t0 += fo::kTcTile) {
             fo::TcTile T{};
             T.L = L;
             T.npairs = std::min(fo::kTcTile, b - t0);
             T.s0 = (long long)sfl;
-            for (int i = 0; i < T.npairs; ++i) {
-                T.coef0[i] = pl->hp[order[t0 + i]].coef0;
-                pmap[order[t0 + i]] = fo::TcPairMap{(long long)sfl, i, T.npairs};
+            for (int i = 0; i < T.npairs; ++i) T.coef0[i] = pl->hp[order[t0 + i]].coef0;
+            const int npg = fo::tc_fft_group(G);
+            for (int q0 = 0; q0 < T.npairs; q0 += npg) {
+                fo::TcFftGroup fg{};
+                fg.s0 = (long long)sfl;
+                fg.L = L;
+                fg.ntile = T.npairs;
+                fg.p0 = q0;
+                fg.npg = std::min(npg, T.npairs - q0);
+                for (int q = 0; q < fg.npg; ++q) fg.pair[q] = order[t0 + q0 + q];
+                fgroups.push_back(fg);
             }
-            sfl += 2ull * G * 2 * T.npairs * W2p;
+            fsm = std::max(fsm, fo::tc_fft_smem(G));
+            sfl += 2ull * G * W2 * 2 * T.npairs;
             tiles.push_back(T);
             tile_L.push_back(L);
         }
@@ -666,11 +676,13 @@ static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
     }
     const size_t bt = tiles.size() * sizeof(fo::TcTile);
     pl->tc_off_items = align256(bt);
-    pl->tc_off_pmap = pl->tc_off_items + align256(items.size() * sizeof(fo::TcItem));
-    pl->tc_meta.assign(pl->tc_off_pmap + pmap.size() * sizeof(fo::TcPairMap), 0);
+    pl->tc_off_groups = pl->tc_off_items + align256(items.size() * sizeof(fo::TcItem));
+    pl->tc_meta.assign(pl->tc_off_groups + fgroups.size() * sizeof(fo::TcFftGroup), 0);
     memcpy(pl->tc_meta.data(), tiles.data(), bt);
     memcpy(pl->tc_meta.data() + pl->tc_off_items, items.data(), items.size() * sizeof(fo::TcItem));
-    memcpy(pl->tc_meta.data() + pl->tc_off_pmap, pmap.data(), pmap.size() * sizeof(fo::TcPairMap));
+    memcpy(pl->tc_meta.data() + pl->tc_off_groups, fgroups.data(), fgroups.size() * sizeof(fo::TcFftGroup));
+    pl->tcb.ngroups = (int)fgroups.size();
+    pl->tcb.fft_smem = fsm;
     pl->tc = true;
     return sfl;
 }

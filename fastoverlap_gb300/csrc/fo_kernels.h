@@ -125,11 +125,20 @@ struct TcTile {
     int bucket;       // index of its table in the launch's TcMaps
     int npairs;       // pairs in the tile (<= kTcTile)
     int pad;
-    long long s0;     // offset (floats) of the tile's sums in S: [col < 2G][row < 2 npairs][mm < W2p]
+    long long s0;     // offset (floats) of the tile's sums in S: [col < 2G][mm < W^2][row < 2 npairs]
     long long coef0[kTcTile];   // complex offset of each pair's coefficients (ilmm layout)
 };
 struct TcItem { int tile, mm0, mm1, pad; };
-struct TcPairMap { long long s0; int row, ntile; };   // its tile's S offset, its row, pairs in the tile
+// Pairs per block of the FFT stage: four (one when G = 2 Jmax + 2 > 32).
+constexpr int kTcFftGroup = 4;
+__host__ __device__ inline int tc_fft_group(int G) { return G <= 32 ? kTcFftGroup : 1; }
+struct TcFftGroup {
+    long long s0;   // its tile's S offset
+    int L;          // Jmax of the tile
+    int ntile;      // pairs in the tile (rows: 2 ntile per column and mm)
+    int p0, npg;    // first pair (row) of the group in the tile, pairs in the group
+    int pair[kTcFftGroup];   // plan index of each pair of the group
+};
 struct TcMaps {
     CUtensorMap map[kTcMaxBuckets];   // Wigner tables [hi|lo][mm][Nr][32] (TMA, 128-byte swizzle)
     int nr[kTcMaxBuckets];            // rows per mm: 2G rounded up to 16
@@ -142,7 +151,9 @@ struct TcBuffers {
     const PairDev *pairs = nullptr;
     const TcTile *tiles = nullptr;
     const TcItem *items = nullptr;
-    const TcPairMap *pmap = nullptr;
+    const TcFftGroup *groups = nullptr;   // FFT-stage blocks
+    int ngroups = 0;
+    size_t fft_smem = 0;                  // dynamic shared memory of the FFT stage
     const void *coef = nullptr;   // complex FP32 coefficients
     float *S = nullptr;           // contraction sums
     void *grid = nullptr;         // FP32 overlap grids
@@ -157,6 +168,7 @@ size_t tc_table_floats(int bw);      // floats of its table
 bool tc_make_table(int bw, const double *d64, float *out, CUtensorMap *map, cudaStream_t s);
 void launch_wigner_tc(const TcBuffers &b, cudaStream_t s);   // the contraction (tcgen05)
 void launch_isoft_tc(const TcBuffers &b, cudaStream_t s);    // the FFT stage after it
+size_t tc_fft_smem(int G);           // its dynamic shared memory for planes of edge G
 
 // context options (library-internal; the server creates worker contexts)
 fo_opts ctx_opts(const fo_ctx *ctx);

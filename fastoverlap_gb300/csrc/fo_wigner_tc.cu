@@ -27,10 +27,10 @@
 // and written to shared memory in the same 128-byte-swizzled K-major layout.
 // A single thread issues the MMAs; four epilogue warps read the accumulators
 // (tcgen05.ld, warp w owns TMEM lanes 32w..32w+31) for four mm at a time and
-// write the sums to S[tile][col][row][mm] (mm fastest, 16-byte stores; rows
-// are the real parts of the tile's pairs, then their imaginary parts, so a
-// tile holds 2 npairs rows), where the FFT kernel below reads each (pair,
-// beta_k) as contiguous runs.
+// write the sums to S[tile][col][mm][row] (rows fastest: the real parts of
+// the tile's pairs, then their imaginary parts, 2 npairs rows), so each warp
+// store covers 128 contiguous bytes; the FFT kernel below reads the rows of a
+// group of pairs for every mm of one beta_k.
 //
 // Every wait on an mbarrier is bounded (about two seconds on the global
 // timer); a wait that runs out sets *err, the CTA leaves its loops, frees its
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const TcItem it = items[blockIdx.x];
     const TcTile &T = tiles[it.tile];
-    const int L = T.L, bw = L + 1, G = 2 * bw, W = 2 * L + 1, W2p = ((W * W + 3) / 4) * 4;
+    const int L = T.L, bw = L + 1, G = 2 * bw, W = 2 * L + 1;
     const int Nr = maps.nr[T.bucket], nks = (bw + 7) / 8, nmm = it.mm1 - it.mm0;
     const int npairs = T.npairs;
     const CUtensorMap *map = &maps.map[T.bucket];
@@ -310,9 +310,9 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         const int row = 32 * warp + lane, p = row & 63, part = row >> 6;
         const bool valid = p < npairs;
         const uint32_t lrow = tbase + ((uint32_t)(32 * warp) << 16);
-        const int ncol = 2 * G;
-        const long long ldm = W2p, cstride = 2LL * npairs * W2p;
-        float *base = S + T.s0 + (long long)(part * npairs + p) * ldm;
+        const int ncol = 2 * G, W2 = W * W;
+        const long long R = 2LL * npairs;   // rows per (col, mm)
+        float *base = S + T.s0 + (part * npairs + p);
         const int nbatch = (nmm + kTcBatch - 1) / kTcBatch;
         for (int q = 0; q < nbatch; ++q) {
             if (!mbar_wait(acc_full, q & 1, abort)) { give_up(); break; }
@@ -330,16 +330,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                     for (int c = 0; c < 16; ++c) {
                         const int col = cc + c;
                         if (col < ncol) {
-                            float *dst = base + (long long)col * cstride + mmq;
-                            if (nb == 4) {
-                                *reinterpret_cast<float4 *>(dst) =
-                                    make_float4(__uint_as_float(v0[c]), __uint_as_float(v1[c]), __uint_as_float(v2[c]),
-                                                __uint_as_float(v3[c]));
-                            } else {
-                                dst[0] = __uint_as_float(v0[c]);
-                                if (nb > 1) dst[1] = __uint_as_float(v1[c]);
-                                if (nb > 2) dst[2] = __uint_as_float(v2[c]);
-                            }
+                            float *dst = base + ((long long)col * W2 + mmq) * R;
+                            dst[0] = __uint_as_float(v0[c]);
+                            if (nb > 1) dst[R] = __uint_as_float(v1[c]);
+                            if (nb > 2) dst[2 * R] = __uint_as_float(v2[c]);
+                            if (nb > 3) dst[3 * R] = __uint_as_float(v3[c]);
                         }
                     }
                 }
@@ -357,43 +352,50 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 }
 
 // ---------------------------------------------------------------------------
-// FFT stage: one block per (beta index k, pair), both orientations: the
-// contraction's sums of the pair's row are contiguous in mm; scattered into
-// the (m1, m2) grid, then the transform tail shared with k_isoft.
-__global__ void __launch_bounds__(256) k_isoft_tc(const PairDev *pairs, const TcPairMap *pmap, const float *S,
+// FFT stage: one block per (beta index k, group of up to four pairs of a
+// tile).  For every mm the group's real and imaginary rows of both
+// orientations' columns are contiguous (4 runs of npg floats); they are
+// scattered into each pair's (m1, m2) planes, then each pair goes through the
+// transform tail shared with k_isoft.
+__global__ void __launch_bounds__(256) k_isoft_tc(const PairDev *pairs, const TcFftGroup *groups, const float *S,
                                                   float *grid) {
     extern __shared__ __align__(16) unsigned char smem_fft[];
-    const int k = blockIdx.x, p = blockIdx.y;
-    const PairDev P = pairs[p];
-    const int G = P.G, L = P.L, Wc = 2 * L + 1, W2 = Wc * Wc, W2p = ((W2 + 3) / 4) * 4;
+    const int k = blockIdx.x;
+    const TcFftGroup Gr = groups[blockIdx.y];
+    const int L = Gr.L, G = 2 * (L + 1), Wc = 2 * L + 1, W2 = Wc * Wc, npg = Gr.npg;
     if (k >= G) return;
-    const bool inv = P.norient == 2;
     const int PL = isoft_plane(G), ld = isoft_ld(G);
-    float2 *bufA = (float2 *)smem_fft, *bufB = bufA + PL, *bufC = bufB + PL, *tw = bufC + PL;
+    float2 *planes = (float2 *)smem_fft;   // pair q: A at 3q PL, Z at (3q + 1) PL, C at (3q + 2) PL
+    float2 *tw = planes + 3 * npg * PL;
     for (int t = threadIdx.x; t < G; t += blockDim.x) {
         float sn, cs;
         sincospif(2.0f * t / G, &sn, &cs);
         tw[t] = make_float2(cs, sn);
     }
-    for (int t = threadIdx.x; t < PL; t += blockDim.x) {
-        bufA[t] = make_float2(0.f, 0.f);
-        bufC[t] = make_float2(0.f, 0.f);
-    }
+    for (int q = 0; q < npg; ++q)
+        for (int t = threadIdx.x; t < PL; t += blockDim.x) {
+            planes[3 * q * PL + t] = make_float2(0.f, 0.f);
+            planes[(3 * q + 2) * PL + t] = make_float2(0.f, 0.f);
+        }
     __syncthreads();
-    const TcPairMap pm = pmap[p];
-    const long long rows = 2LL * pm.ntile;   // rows per column of the pair's tile
-    const float *re0 = S + pm.s0 + ((long long)k * rows + pm.row) * W2p;
-    const float *im0 = re0 + (long long)pm.ntile * W2p;
-    const float *re1 = re0 + (long long)G * rows * W2p, *im1 = re1 + (long long)pm.ntile * W2p;
-    for (int t = threadIdx.x; t < W2; t += blockDim.x) {
-        const int i1 = t / Wc, i2 = t % Wc;
+    const long long R = 2LL * Gr.ntile;
+    const float *c0 = S + Gr.s0 + (long long)k * W2 * R + Gr.p0;        // column k (direct)
+    const float *c1 = S + Gr.s0 + (long long)(G + k) * W2 * R + Gr.p0;  // column G + k (inverted)
+    for (int t = threadIdx.x; t < W2 * npg; t += blockDim.x) {
+        const int mm = t / npg, q = t % npg;
+        const int i1 = mm / Wc, i2 = mm % Wc;
         const int m1 = (i1 <= L) ? i1 : i1 - Wc, m2 = (i2 <= L) ? i2 : i2 - Wc;
         const int dst = ((m1 + G) % G) * ld + (m2 + G) % G;
-        bufA[dst] = make_float2(re0[t], im0[t]);
-        if (inv) bufC[dst] = make_float2(re1[t], im1[t]);
+        const long long o = (long long)mm * R + q;
+        planes[3 * q * PL + dst] = make_float2(c0[o], c0[o + Gr.ntile]);
+        planes[(3 * q + 2) * PL + dst] = make_float2(c1[o], c1[o + Gr.ntile]);
     }
     __syncthreads();
-    isoft_tail<float, float2>(bufA, bufB, bufC, tw, G, k, inv, grid + P.grid0);
+    for (int q = 0; q < npg; ++q) {
+        const PairDev &P = pairs[Gr.pair[q]];
+        isoft_tail<float, float2>(planes + 3 * q * PL, planes + (3 * q + 1) * PL, planes + (3 * q + 2) * PL, tw, G,
+                                  k, P.norient == 2, grid + P.grid0);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -471,10 +473,11 @@ void launch_wigner_tc(const TcBuffers &b, cudaStream_t s) {
     }
 }
 
+size_t tc_fft_smem(int G) { return sizeof(float2) * (3ull * tc_fft_group(G) * isoft_plane(G) + G); }
+
 void launch_isoft_tc(const TcBuffers &b, cudaStream_t s) {
-    const size_t fsm = sizeof(float2) * (3 * isoft_plane(b.maxG) + b.maxG);
     allow_max_smem<k_isoft_tc>();
-    k_isoft_tc<<<dim3(b.maxG, b.npairs), 256, fsm, s>>>(b.pairs, b.pmap, b.S, (float *)b.grid);
+    k_isoft_tc<<<dim3(b.maxG, b.ngroups), 256, b.fft_smem, s>>>(b.pairs, b.groups, b.S, (float *)b.grid);
 }
 
 }  // namespace fo
