@@ -284,10 +284,13 @@ RefAssign ref_assign(int n, int maxg, bool fp32, bool recomp, double dmax) {
     if (L.coord_end + L.lap_end <= kRefSmemCap) {
         r.smem = up(L.coord_end + L.lap_end);
         r.lapstride = 0;
-    } else if (L.coord_end + L.lap_small <= kRefSplitCap) {
-        // the assignment's random-access arrays and the neighbour-selection
-        // scratch stay on chip; the row-major neighbour lists (read a row at
-        // a time) go to the candidate's global scratch
+    } else if (recomp && L.coord_end + L.lap_small <= kRefSplitCap) {
+        // mixed form: the assignment's random-access arrays and the
+        // neighbour-selection scratch stay on chip; the row-major neighbour
+        // lists (read a row at a time) go to the candidate's global scratch.
+        // (The FP64 form keeps its stored costs and everything else in global
+        // scratch: its small on-chip part lets 16 warps share an SM, which
+        // measured faster than the split's 5.)
         r.smem = up(L.coord_end + L.lap_small);
         r.lapstride = (long long)((L.lap_end + 255) & ~(size_t)255);
         r.split = 1;
@@ -473,6 +476,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     size_t o_cdist = cv.take<double>(nc), o_cR = cv.take<double>(9 * (size_t)nc),
            o_cdisp = cv.take<double>(3 * (size_t)nc);
     size_t o_cxyz = cv.take<double>(3 * candatoms), o_cperm = cv.take<int>(candatoms);
+    size_t o_cthr = cv.take<float>(pl->fp32 ? candatoms : 0);
     size_t o_cnit = cv.take<int>(nc), o_cst = cv.take<int>(nc);
     size_t o_res = cv.take<fo_pair_result>(np), o_al = cv.take<double>(3 * (size_t)ns),
            o_pb = cv.take<int>(ns);
@@ -554,6 +558,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     r.cR = (double *)P(o_cR);
     r.cdisp = (double *)P(o_cdisp);
     r.cxyz = (double *)P(o_cxyz);
+    r.cthr = (float *)P(o_cthr);
     r.cperm = (int *)P(o_cperm);
     r.cniter = (int *)P(o_cnit);
     r.cstat = (int *)P(o_cst);

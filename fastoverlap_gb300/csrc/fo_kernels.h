@@ -96,6 +96,7 @@ struct RefineBuffers {
     unsigned char *lap;     // LAP scratch
     double *cdist, *cR, *cdisp, *cxyz;
     int *cperm, *cniter, *cstat;
+    float *cthr;            // per candidate atom: its neighbour-list threshold (mixed form)
     // final outputs
     void *results;          // fo_pair_result[npairs]
     double *aligned;        // 3 per atom, original order

@@ -849,18 +849,24 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
 // The m nearest columns of one row (mixed form): the m smallest squared
 // distances dist(j), j < ns (m < ns), as column indices in increasing order;
 // ties at the m-th value go to the lowest indices.  The whole warp works on
-// the row: the distances go to the scratch d (ns floats), the m-th smallest
-// is found by bisection on their bit patterns (non-negative floats order like
-// their bits) with warp-wide counts, and the chosen columns are compacted in
-// column order.  It picks the same set as the PAIRDISTS heap whenever the
-// m-th and (m+1)-th distances differ; the order within the row only decides
-// between tied optimal assignments.  The bisection stops as soon as a
-// threshold has exactly m distances below it.
+// the row: the distances go to the scratch d (ns floats) unless they fit in
+// registers, and the m-th smallest is found by bisection on their bit
+// patterns (non-negative floats order like their bits) with warp-wide counts,
+// keeping count(< lo) <= m < count(< hi); it stops as soon as a threshold has
+// exactly m distances below it.  The chosen columns are compacted in column
+// order.  It picks the same set as the PAIRDISTS heap whenever the m-th and
+// (m+1)-th distances differ; the order within the row only decides between
+// tied optimal assignments.
+// thr (optional): this row's m-th distance from the previous call.  When it
+// is > 0 the bisection starts from the bracket [0.99 thr, 1.01 thr], which
+// usually holds the new m-th distance (the structures move little between
+// iterations) and gives the same result in a few counts instead of ~20.  The
+// new m-th distance (or exact threshold) is stored back.
 // Rows of up to 32*kNearReg columns keep their distances in registers.
 constexpr int kNearReg = 16;
 
 template <typename KT, typename DF>
-__device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, const DF &dist) {
+__device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, const DF &dist, float *thr = nullptr) {
     const int lane = threadIdx.x & 31;
     const unsigned ltmask = (1u << lane) - 1u;
     const bool inreg = ns <= 32 * kNearReg;
@@ -883,16 +889,35 @@ __device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, cons
         }
         return (int)__reduce_add_sync(kFull, (unsigned)c);
     };
-    unsigned v = 0;   // grows to the m-th smallest bit pattern
+    unsigned lo = 0, hi = 0x7f800000u, v = 0;   // count(< 0) = 0 <= m < ns = count(< +inf)
     bool exact = false;
-    for (int b = 30; b >= 0; --b) {
-        const unsigned t = v | (1u << b);
-        const int c = count_below(t);
-        if (c <= m) v = t;
-        if (c == m) { exact = true; break; }   // {d < t} holds exactly m columns
+    const float g = thr ? *thr : 0.f;
+    if (g > 0.f) {
+        const unsigned a = __float_as_uint(g * 0.99f), b = __float_as_uint(g * 1.01f);
+        const int ca = count_below(a);
+        if (ca == m) { exact = true; v = a; }
+        else if (ca > m) hi = a;
+        else {
+            lo = a;
+            const int cb = count_below(b);
+            if (cb == m) { exact = true; v = b; }
+            else if (cb > m) hi = b;
+            else lo = b;
+        }
+    }
+    while (!exact && hi - lo > 1u) {
+        const unsigned mid = lo + (hi - lo) / 2u;
+        const int c = count_below(mid);
+        if (c == m) { exact = true; v = mid; }
+        else if (c < m) lo = mid;
+        else hi = mid;
     }
     int need_eq = 0, out = 0;
-    if (!exact) need_eq = m - count_below(v);   // v is the m-th smallest: ties at v, lowest index first
+    if (!exact) {   // lo is the m-th smallest: ties at lo, lowest index first
+        v = lo;
+        need_eq = m - count_below(v);
+    }
+    if (thr && lane == 0) *thr = __uint_as_float(v);
     for (int b0 = 0; b0 < ns; b0 += 32) {
         const int j = b0 + lane;
         unsigned u = 0xffffffffu;
@@ -933,7 +958,7 @@ struct GroupCoords {
 // JOVOSAP for one group).  Returns the assignment's status.
 template <typename KT, typename DT, typename CT, bool RECOMP, bool BOX>
 __device__ int assign_group(const int ns, const int m, const GroupCoords &G, unsigned char *lb, unsigned char *lbk,
-                            const RefLayout &L) {
+                            const RefLayout &L, float *thr = nullptr, bool warm = false) {
     const int lane = threadIdx.x & 31;
     const bool dense = (m == ns);
     constexpr bool kF32 = sizeof(DT) == 4;   // mixed form: no augmenting row reduction
@@ -945,14 +970,17 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
     if constexpr (RECOMP) {
         auto run = [&](const auto &cf) {
             if (!dense) {
-                if (ns <= kHeapMaxRow) {   // a heap per lane, one row each
+                if (ns <= kHeapMaxRow && !warm) {   // first pass: a heap per lane, one row each
                     float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
-                    for (int i = lane; i < ns; i += 32)
+                    for (int i = lane; i < ns; i += 32) {
                         nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
-                } else {                   // the warp on one row at a time
+                        if (thr) thr[i] = hd[0];   // the heap's root: the row's m-th distance
+                    }
+                } else {   // the warp on one row at a time, from the row's last m-th distance when warm
                     float *dr = (float *)(lb + L.lap_heap);
                     for (int i = 0; i < ns; ++i)
-                        nearest_warp<KT>(kk + i * m, dr, ns, m, [&](int j) { return cf.d2(i, j); });
+                        nearest_warp<KT>(kk + i * m, dr, ns, m, [&](int j) { return cf.d2(i, j); },
+                                         thr ? thr + i : nullptr);
                 }
             }
             __syncwarp();
@@ -1023,7 +1051,7 @@ template <typename DT, typename CT, bool RECOMP, bool BOX>
 __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
     const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
     const double *xa, const double *xb, const double *peaks, const int *npeaks, unsigned char *lapg,
-    double *cdist, double *cR, double *cdisp, double *cxyz, int *cperm, int *cniter, int *cstat) {
+    double *cdist, double *cR, double *cdisp, double *cxyz, int *cperm, int *cniter, int *cstat, float *cthr) {
     constexpr bool kF32 = sizeof(DT) == 4;
     static_assert(kF32 || !RECOMP, "costs are recomputed only from FP32 coordinates");
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1057,6 +1085,7 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
         // Mixed form: FP32 coordinates for the costs, FP64 superposition built
         // from few FP64 instructions (Horn rotation, one affine map per step).
         __shared__ double sRb[9], sRn[9], sRc[9], sRs[9], sT[12], sF[8];
+        float *thrc = cthr + ob;   // per row: its m-th neighbour distance in the last iteration
         GroupCoords GC;
         GC.bulk = bulk;
         GC.xb = XB;
@@ -1191,8 +1220,8 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
                 GC.A = DA + 3 * s0;
                 GC.B4 = B4 + s0;
                 GC.A4 = A4 + s0;
-                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L)
-                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L);
+                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0)
+                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0);
                 if (rc) fail += 1;
                 __syncwarp();
                 for (int i = lane; i < ns; i += 32) {
@@ -1644,7 +1673,7 @@ void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux,
         allow_max_smem<k_refine_warp<DT, CT, RC, BX>>();                                             \
         k_refine_warp<DT, CT, RC, BX><<<bk.count, 32, bk.smem, s>>>(                                  \
             b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,      \
-            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat);                                       \
+            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat, b.cthr);                               \
     } while (0)
         if (b.fp32 && b.recomp) {
             if (b.bulk) {
