@@ -338,6 +338,7 @@ def main():
     ap.add_argument("--npairs", type=int, default=4096)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="time eager launches instead of graph replay")
     ap.add_argument("--plain-sample", type=int, default=32)
     ap.add_argument("--c3-pairs", type=int, default=64, help="0 skips the large-bandwidth study")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
@@ -365,7 +366,18 @@ def main():
     for _ in range(args.warmup):
         batch.plan_run()
         batch.plan_wait()
+    # per-kernel breakdown from one eager step (CUDA events between launches)
     ctx.profile_reset()
+    ctx.flush_l2(512 << 20)
+    batch.plan_run()
+    batch.plan_wait()
+    prof = ctx.profile()
+    if not args.no_graph:
+        # the timed steps replay the plan as one captured CUDA graph (this run
+        # goes eagerly and captures it)
+        batch.plan_graph(True)
+        batch.plan_run()
+        batch.plan_wait()
     clocks = ClockSampler(local)
     barrier(dist)
     ctx.synchronize()
@@ -381,7 +393,6 @@ def main():
     ctx.synchronize()
     barrier(dist)
     clk = clocks.stop()
-    prof = ctx.profile()
     res = batch.plan_results(with_coords=True)
     tot_ms = allmax(dist, sum(step_ms))
     value = args.npairs * ws * args.steps / (tot_ms / 1000.0)
@@ -516,6 +527,9 @@ def main():
             "data": "synthetic",
             "config": dict({"workload": WORKLOAD, "npairs_per_gpu": args.npairs,
                             "precision": args.precision, "l2": "flushed (512 MiB write) between steps",
+                            "launch": ("eager launches" if args.no_graph else
+                                       "one CUDA-graph replay of the plan per step (kernel breakdown from an "
+                                       "eager step)"),
                             "kernel_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in kern.items()}},
                            **cfg_extra),
             "roofline": roof, "cpu_baseline": cpu,
