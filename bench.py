@@ -339,6 +339,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="time eager launches instead of graph replay")
+    ap.add_argument("--no-tensor-cores", action="store_true",
+                    help="mixed form: Wigner contraction on CUDA cores instead of tcgen05")
     ap.add_argument("--plain-sample", type=int, default=32)
     ap.add_argument("--c3-pairs", type=int, default=64, help="0 skips the large-bandwidth study")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
@@ -356,7 +358,8 @@ def main():
     import fastoverlap_gb300 as F
     from fastoverlap_gb300.batch import ClusterBatch
 
-    ctx = F.Context(device=local, precision=args.precision, profile=True)
+    ctx = F.Context(device=local, precision=args.precision, profile=True,
+                    tensor_cores=not args.no_tensor_cores)
     pos1 = [p[0] for p in pairs]
     pos2 = [p[1] for p in pairs]
     perms = [p[2] for p in pairs]

@@ -131,7 +131,10 @@ struct TcTile {
 };
 struct TcItem { int tile, mm0, mm1, pad; };
 // Pairs per block of the FFT stage: four (one when G = 2 Jmax + 2 > 32).
-constexpr int kTcFftGroup = 4;
+#ifndef FO_TC_FFT_GROUP
+#define FO_TC_FFT_GROUP 4
+#endif
+constexpr int kTcFftGroup = FO_TC_FFT_GROUP;
 __host__ __device__ inline int tc_fft_group(int G) { return G <= 32 ? kTcFftGroup : 1; }
 struct TcFftGroup {
     long long s0;   // its tile's S offset

@@ -857,8 +857,8 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
 // order.  It picks the same set as the PAIRDISTS heap whenever the m-th and
 // (m+1)-th distances differ; the order within the row only decides between
 // tied optimal assignments.
-// thr (optional): this row's m-th distance from the previous call.  When it
-// is > 0 the bisection starts from the bracket [0.99 thr, 1.01 thr], which
+// thr (optional): this row's m-th distance from the previous call; with warm
+// set, the bisection starts from the bracket [0.99 thr, 1.01 thr], which
 // usually holds the new m-th distance (the structures move little between
 // iterations) and gives the same result in a few counts instead of ~20.  The
 // new m-th distance (or exact threshold) is stored back.
@@ -866,7 +866,8 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
 constexpr int kNearReg = 16;
 
 template <typename KT, typename DF>
-__device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, const DF &dist, float *thr = nullptr) {
+__device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, const DF &dist, float *thr = nullptr,
+                             bool warm = false) {
     const int lane = threadIdx.x & 31;
     const unsigned ltmask = (1u << lane) - 1u;
     const bool inreg = ns <= 32 * kNearReg;
@@ -891,7 +892,7 @@ __device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, cons
     };
     unsigned lo = 0, hi = 0x7f800000u, v = 0;   // count(< 0) = 0 <= m < ns = count(< +inf)
     bool exact = false;
-    const float g = thr ? *thr : 0.f;
+    const float g = (thr && warm) ? *thr : 0.f;
     if (g > 0.f) {
         const unsigned a = __float_as_uint(g * 0.99f), b = __float_as_uint(g * 1.01f);
         const int ca = count_below(a);
@@ -970,17 +971,15 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
     if constexpr (RECOMP) {
         auto run = [&](const auto &cf) {
             if (!dense) {
-                if (ns <= kHeapMaxRow && !warm) {   // first pass: a heap per lane, one row each
+                if (ns <= kHeapMaxRow) {   // a heap per lane, one row each (32 rows at once)
                     float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
-                    for (int i = lane; i < ns; i += 32) {
+                    for (int i = lane; i < ns; i += 32)
                         nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
-                        if (thr) thr[i] = hd[0];   // the heap's root: the row's m-th distance
-                    }
                 } else {   // the warp on one row at a time, from the row's last m-th distance when warm
                     float *dr = (float *)(lb + L.lap_heap);
                     for (int i = 0; i < ns; ++i)
                         nearest_warp<KT>(kk + i * m, dr, ns, m, [&](int j) { return cf.d2(i, j); },
-                                         thr ? thr + i : nullptr);
+                                         thr ? thr + i : nullptr, warm);
                 }
             }
             __syncwarp();
