@@ -39,6 +39,11 @@
 #ifndef FO_MIXED_ARR
 #define FO_MIXED_ARR 0
 #endif
+// 1: dense groups of the mixed form use the register-resident assignment
+// (jv_dense_reg) instead of the sequential method's warp form
+#ifndef FO_DENSE_REG
+#define FO_DENSE_REG 1
+#endif
 
 namespace fo {
 
@@ -460,6 +465,87 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
         }
         if (__shfl_sync(kFull, fail, 0)) return 6;
         __syncwarp();
+    }
+    return 0;
+}
+
+// Dense assignment of the mixed form (groups of at most 64 atoms, every
+// column in every row), one warp, the columns in registers: lane l owns
+// columns l and l + 32 (price, distance label, scanned flag, owning row).
+// Column reduction (each column to its cheapest row, a row keeping the
+// highest of its columns), then for every free row a Dijkstra search for the
+// shortest augmenting path (Jonker & Volgenant, Computing 38, 1987, the
+// shortest-path phase): each step is one warp minimum over the unscanned
+// columns (lowest column on ties) and one relaxation of the owning row's
+// costs by every lane; prices of the scanned columns move by d_j - d_end and
+// the path is flipped.  The result is an optimal assignment -- the same one
+// as the sequential method's whenever the optimum is unique; only the choice
+// among tied optima may differ.  x (shared, n ints) receives row -> column.
+// Returns 0, or 4 if a search ends without a free column (cannot happen for a
+// complete cost matrix).
+template <typename CF>
+__device__ int jv_dense_reg(const int n, const CF &cost, int *x) {
+    const int lane = threadIdx.x & 31, j0 = lane, j1 = lane + 32;
+    const bool has0 = j0 < n, has1 = j1 < n;
+    long long v0 = kBigInt, v1 = kBigInt;
+    int y0 = -1, y1 = -1;
+    for (int i = 0; i < n; ++i) {
+        if (has0) { const long long c = cost(i, j0, j0); if (c < v0) { v0 = c; y0 = i; } }
+        if (has1) { const long long c = cost(i, j1, j1); if (c < v1) { v1 = c; y1 = i; } }
+    }
+    for (int i = lane; i < n; i += 32) x[i] = -1;
+    __syncwarp();
+    if (has0) atomicMax(&x[y0], j0);
+    if (has1) atomicMax(&x[y1], j1);
+    __syncwarp();
+    if (has0 && x[y0] != j0) y0 = -1;
+    if (has1 && x[y1] != j1) y1 = -1;
+    __syncwarp();
+    for (int i0 = 0; i0 < n; ++i0) {
+        if (x[i0] >= 0) continue;
+        long long d0 = has0 ? cost(i0, j0, j0) - v0 : kLLMax, d1 = has1 ? cost(i0, j1, j1) - v1 : kLLMax;
+        int lab0 = i0, lab1 = i0;
+        bool sc0 = !has0, sc1 = !has1;
+        long long mn = 0;
+        int jend = -1;
+        for (int step = 0; step <= n; ++step) {
+            const unsigned long long k0 = sc0 ? kNoKey : ((unsigned long long)(d0 + kKeyBias) << 6) | (unsigned)j0;
+            const unsigned long long k1 = sc1 ? kNoKey : ((unsigned long long)(d1 + kKeyBias) << 6) | (unsigned)j1;
+            const unsigned long long km = wmin_u64(k0 < k1 ? k0 : k1);
+            if (km == kNoKey) break;
+            const int jm = (int)(km & 63u), own = jm & 31;
+            const bool hi = jm >= 32;
+            mn = (long long)(km >> 6) - kKeyBias;
+            const int yj = __shfl_sync(kFull, hi ? y1 : y0, own);
+            const long long vj = __shfl_sync(kFull, hi ? v1 : v0, own);
+            if (lane == own) {
+                if (hi) sc1 = true;
+                else sc0 = true;
+            }
+            if (yj < 0) { jend = jm; break; }
+            const long long h = cost(yj, jm, jm) - vj - mn;   // the same on every lane
+            if (!sc0) { const long long nd = cost(yj, j0, j0) - v0 - h; if (nd < d0) { d0 = nd; lab0 = yj; } }
+            if (!sc1) { const long long nd = cost(yj, j1, j1) - v1 - h; if (nd < d1) { d1 = nd; lab1 = yj; } }
+        }
+        if (jend < 0) return 4;
+        if (has0 && sc0) v0 += d0 - mn;
+        if (has1 && sc1) v1 += d1 - mn;
+        int j = jend;
+        for (int guard = 0; guard <= n; ++guard) {
+            const int own = j & 31;
+            const bool hi = j >= 32;
+            const int i = __shfl_sync(kFull, hi ? lab1 : lab0, own);
+            if (lane == own) {
+                if (hi) y1 = i;
+                else y0 = i;
+            }
+            const int next = x[i];
+            __syncwarp();
+            if (lane == 0) x[i] = j;
+            __syncwarp();
+            if (i == i0) break;
+            j = next;
+        }
     }
     return 0;
 }
@@ -983,6 +1069,9 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                 }
             }
             __syncwarp();
+#if FO_DENSE_REG
+            if (dense && ns <= 64) return jv_dense_reg(ns, cf, x);
+#endif
             return jv_warp<!kF32 || FO_MIXED_ARR, KT>(ns, m, dense, cf, kk, v, dd, x, y, lab, fr, todo, ok);
         };
         return run(CostF32<CT, BOX>{G.B4, G.A4, {G.bxf[0], G.bxf[1], G.bxf[2]}, {G.rxf[0], G.rxf[1], G.rxf[2]}});
