@@ -44,11 +44,6 @@
 #ifndef FO_DENSE_REG
 #define FO_DENSE_REG 1
 #endif
-// 1: sparse groups of the mixed form up to kSparseRegMax atoms use the
-// register-resident assignment (jv_sparse_reg) over the neighbour lists
-#ifndef FO_SPARSE_REG
-#define FO_SPARSE_REG 1
-#endif
 
 namespace fo {
 
@@ -543,141 +538,6 @@ __device__ int jv_dense_reg(const int n, const CF &cost, int *x) {
             if (lane == own) {
                 if (hi) y1 = i;
                 else y0 = i;
-            }
-            const int next = x[i];
-            __syncwarp();
-            if (lane == 0) x[i] = j;
-            __syncwarp();
-            if (i == i0) break;
-            j = next;
-        }
-    }
-    return 0;
-}
-
-// Sparse assignment of the mixed form for groups of at most 160 atoms: the
-// same register-resident shortest-augmenting-path search as jv_dense_reg,
-// with five columns per lane (lane l owns columns l + 32 s, s < 5) and the
-// rows' neighbour lists as a membership bitmap bm (n rows of ceil(n / 32)
-// words, shared): an entry outside a row's list is no edge.  Column
-// reduction over the listed entries (first row wins, a row keeps the highest
-// of its columns), then one Dijkstra search per free row.  Returns 0; 1 when
-// a column is in no row's list, 4 when a search finds no free column (the
-// sparse problem has no complete assignment) -- the caller then runs the
-// sequential method, which reports the same.
-constexpr long long kKeyBias8 = 1LL << 50;   // keys ((d + bias) << 8) | column, column < 256
-
-template <typename KT, typename CF>
-__device__ int jv_sparse_reg(const int n, const int m, const CF &cost, const KT *__restrict__ kk, unsigned *bm,
-                             int *x) {
-    constexpr int S = (kSparseRegMax + 31) / 32;
-    const int lane = threadIdx.x & 31, nw = (n + 31) / 32;
-    for (int q = lane; q < n * nw; q += 32) bm[q] = 0u;
-    __syncwarp();
-    for (int i = 0; i < n; ++i)
-        for (int t = lane; t < m; t += 32) {
-            const int j = (int)kk[i * m + t];
-            atomicOr(&bm[i * nw + (j >> 5)], 1u << (j & 31));
-        }
-    __syncwarp();
-    long long v[S], d[S];
-    int y[S], lab[S];
-    bool sc[S];
-#pragma unroll
-    for (int s = 0; s < S; ++s) { v[s] = kBigInt; y[s] = -1; }
-    for (int i = 0; i < n; ++i) {
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const int c = lane + 32 * s;
-            if (s < nw && c < n && ((bm[i * nw + s] >> lane) & 1u)) {
-                const long long cc = cost(i, c, c);
-                if (cc < v[s]) { v[s] = cc; y[s] = i; }
-            }
-        }
-    }
-    int bad = 0;
-#pragma unroll
-    for (int s = 0; s < S; ++s)
-        if (lane + 32 * s < n && y[s] < 0) bad = 1;
-    if (__any_sync(kFull, bad)) return 1;
-    for (int i = lane; i < n; i += 32) x[i] = -1;
-    __syncwarp();
-#pragma unroll
-    for (int s = 0; s < S; ++s)
-        if (lane + 32 * s < n) atomicMax(&x[y[s]], lane + 32 * s);
-    __syncwarp();
-#pragma unroll
-    for (int s = 0; s < S; ++s)
-        if (lane + 32 * s < n && x[y[s]] != lane + 32 * s) y[s] = -1;
-    __syncwarp();
-    auto pick_int = [&](const int (&a)[S], int s) {
-        int r = a[0];
-#pragma unroll
-        for (int q = 1; q < S; ++q)
-            if (q == s) r = a[q];
-        return r;
-    };
-    auto pick_ll = [&](const long long (&a)[S], int s) {
-        long long r = a[0];
-#pragma unroll
-        for (int q = 1; q < S; ++q)
-            if (q == s) r = a[q];
-        return r;
-    };
-    for (int i0 = 0; i0 < n; ++i0) {
-        if (x[i0] >= 0) continue;
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const int c = lane + 32 * s;
-            const bool valid = s < nw && c < n;
-            sc[s] = !valid;
-            lab[s] = i0;
-            d[s] = (valid && ((bm[i0 * nw + s] >> lane) & 1u)) ? cost(i0, c, c) - v[s] : kLLMax;
-        }
-        long long mn = 0;
-        int jend = -1;
-        for (int step = 0; step <= n; ++step) {
-            unsigned long long kl = kNoKey;
-#pragma unroll
-            for (int s = 0; s < S; ++s)
-                if (!sc[s] && d[s] != kLLMax) {
-                    const unsigned long long k = ((unsigned long long)(d[s] + kKeyBias8) << 8) | (unsigned)(lane + 32 * s);
-                    kl = k < kl ? k : kl;
-                }
-            const unsigned long long km = wmin_u64(kl);
-            if (km == kNoKey) break;
-            const int jm = (int)(km & 255u), own = jm & 31, slot = jm >> 5;
-            mn = (long long)(km >> 8) - kKeyBias8;
-            const int yj = __shfl_sync(kFull, pick_int(y, slot), own);
-            const long long vj = __shfl_sync(kFull, pick_ll(v, slot), own);
-            if (lane == own) {
-#pragma unroll
-                for (int s = 0; s < S; ++s)
-                    if (s == slot) sc[s] = true;
-            }
-            if (yj < 0) { jend = jm; break; }
-            const long long h = cost(yj, jm, jm) - vj - mn;
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-                const int c = lane + 32 * s;
-                if (!sc[s] && ((bm[yj * nw + (s < nw ? s : 0)] >> lane) & 1u)) {
-                    const long long nd = cost(yj, c, c) - v[s] - h;
-                    if (nd < d[s]) { d[s] = nd; lab[s] = yj; }
-                }
-            }
-        }
-        if (jend < 0) return 4;
-#pragma unroll
-        for (int s = 0; s < S; ++s)
-            if (lane + 32 * s < n && sc[s]) v[s] += d[s] - mn;
-        int j = jend;
-        for (int guard = 0; guard <= n; ++guard) {
-            const int own = j & 31, slot = j >> 5;
-            const int i = __shfl_sync(kFull, pick_int(lab, slot), own);
-            if (lane == own) {
-#pragma unroll
-                for (int s = 0; s < S; ++s)
-                    if (s == slot) y[s] = i;
             }
             const int next = x[i];
             __syncwarp();
@@ -1211,12 +1071,6 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
             __syncwarp();
 #if FO_DENSE_REG
             if (dense && ns <= 64) return jv_dense_reg(ns, cf, x);
-#endif
-#if FO_SPARSE_REG
-            if (!dense && ns <= kSparseRegMax) {
-                if (jv_sparse_reg<KT>(ns, m, cf, kk, (unsigned *)(lb + L.lap_bm), x) == 0) return 0;
-                __syncwarp();   // no complete assignment from the lists: the sequential method decides
-            }
 #endif
             return jv_warp<!kF32 || FO_MIXED_ARR, KT>(ns, m, dense, cf, kk, v, dd, x, y, lab, fr, todo, ok);
         };

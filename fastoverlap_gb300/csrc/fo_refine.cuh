@@ -9,7 +9,6 @@ struct RefLayout {
     size_t DBf, DAf, perm, nperm, ptmp, coord_end;
     size_t lap_cc, lap_kk, lap_heap, lap_v, lap_d, lap_x, lap_y, lap_lab, lap_fr, lap_todo, lap_ok, lap_end;
     size_t lap_small;   // bytes of the assignment block before the costs and neighbour lists
-    size_t lap_bm;      // neighbour-list membership bitmap (mixed form, sparse groups <= kSparseRegMax)
     int kkbytes;   // bytes per neighbour-list column index
 };
 
@@ -19,9 +18,6 @@ struct RefLayout {
 // warp on one row at a time (one row of distances as scratch).
 constexpr int kHeapMaxRow = 256;
 constexpr int kHeapStride = 61;
-// Sparse groups of the mixed form up to this size use the register-resident
-// assignment (five columns per lane) over a membership bitmap of the lists.
-constexpr int kSparseRegMax = 160;
 
 __host__ __device__ inline size_t ref_a16(size_t b) { return (b + 15) & ~(size_t)15; }
 
@@ -69,8 +65,6 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     }
     const size_t heap_end = L.lap_heap + scratch;
     if (heap_end > p) p = heap_end;
-    L.lap_bm = p;
-    if (recomp && sparse && maxg <= kSparseRegMax) p += ref_a16(4 * (size_t)maxg * ((maxg + 31) / 32));
     L.lap_small = p;
     L.lap_cc = p; p += recomp ? 0 : ref_a16((size_t)ctsize * maxg * m);
     L.lap_kk = p; p += sparse ? ref_a16((size_t)L.kkbytes * maxg * m) : 0;
