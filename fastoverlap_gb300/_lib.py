@@ -97,6 +97,8 @@ EXPORTS = {
     "fo_last_error": (ctypes.c_char_p, [_vp]),
     "fo_set_precision": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fo_set_tensor_cores": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fo_set_autotune": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fo_plan_tile_shape": (ctypes.c_int, [_vp, _ip, _ip]),
     "fo_cluster_align_batch": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
                                               ctypes.c_int, _dp, _ip, _vp]),
     "fo_bulk_align_batch": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
@@ -260,6 +262,10 @@ class Context(object):
     def set_precision(self, precision):
         self.check(self.lib.fo_set_precision(self.h, _prec(precision)))
         self.precision = precision
+
+    def set_autotune(self, on):
+        """Mixed form: time the tensor-core tile shapes of new plan shapes (default) or not."""
+        self.check(self.lib.fo_set_autotune(self.h, int(bool(on))))
 
     def set_tensor_cores(self, on):
         """Mixed form: Wigner contraction on the tcgen05 tensor cores (default) or not."""

@@ -125,6 +125,12 @@ class _BatchBase(object):
     def plan_device_bytes(self):
         return int(self.ctx.lib.fo_plan_device_bytes(self.plan_h))
 
+    def plan_tile_shape(self):
+        """(chunk, group) of the tensor-core stage ((0, 0) when not used)."""
+        c, g = ctypes.c_int(0), ctypes.c_int(0)
+        self.ctx.check(self.ctx.lib.fo_plan_tile_shape(self.plan_h, ctypes.byref(c), ctypes.byref(g)), "tile shape")
+        return c.value, g.value
+
     def plan_launches(self):
         """Kernel launches one plan_run issues."""
         return int(self.ctx.lib.fo_plan_launches(self.plan_h))

@@ -51,6 +51,8 @@ struct fo_ctx {
     std::string err;
     std::map<int, std::pair<double *, float *>> dtab;
     int tc = 1;   // mixed form: Wigner contraction on the tensor cores
+    int autotune = 1;   // pick the tensor-core tile shape per plan shape by timing
+    std::map<std::string, std::pair<int, int>> tc_shapes;   // plan shape -> (chunk, FFT group)
     std::map<int, std::pair<float *, CUtensorMap>> dtc;   // per bandwidth: its tables in the MMA layout
     double **d_dtab64 = nullptr;
     float **d_dtab32 = nullptr;
@@ -101,6 +103,10 @@ struct fo_plan {
     fo::TcBuffers tcb;
     std::vector<unsigned char> tc_meta;         // tiles, items, pair map (host copy, uploaded once)
     size_t tc_off_items = 0, tc_off_groups = 0;   // their offsets in tc_meta (tiles at 0)
+    unsigned char *tc_meta_dev = nullptr;        // device copy (capacity for every shape tried)
+    std::vector<fo::TcTile> tc_tiles;            // host tiles; tc_tile_t0[t]: first of its pairs in tc_order
+    std::vector<int> tc_tile_t0, tc_order;
+    int tc_chunk = 0, tc_group = 0;              // the tile shape in use
 };
 
 namespace {
@@ -441,6 +447,19 @@ fo_status fo_set_tensor_cores(fo_ctx *ctx, int on) {
     return FO_OK;
 }
 
+fo_status fo_set_autotune(fo_ctx *ctx, int on) {
+    if (!ctx) return FO_ERR_BAD_ARGS;
+    ctx->autotune = on ? 1 : 0;
+    return FO_OK;
+}
+
+fo_status fo_plan_tile_shape(const fo_plan *pl, int *chunk, int *group) {
+    if (!pl || !chunk || !group) return FO_ERR_BAD_ARGS;
+    *chunk = pl->tc ? pl->tc_chunk : 0;
+    *group = pl->tc ? pl->tc_group : 0;
+    return FO_OK;
+}
+
 fo_status fo_set_precision(fo_ctx *ctx, int precision) {
     if (!ctx || (precision != FO_PREC_FP64 && precision != FO_PREC_MIXED)) return FO_ERR_BAD_ARGS;
     ctx->opts.precision = precision;
@@ -580,6 +599,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     if (tc_meta_bytes) {
         fo::TcBuffers &t = pl->tcb;
         unsigned char *mb = (unsigned char *)P(o_tcm);
+        pl->tc_meta_dev = mb;
         t.tiles = (const fo::TcTile *)mb;
         t.items = (const fo::TcItem *)(mb + pl->tc_off_items);
         t.groups = (const fo::TcFftGroup *)(mb + pl->tc_off_groups);
@@ -609,21 +629,25 @@ static bool packed_in_order(const PairT *pairs, int npairs) {
 }
 }
 
+// Tile shapes the autotuner tries: (m1, m2) combinations per contraction
+// CTA and pairs per FFT block.
+constexpr int kTcChunks[] = {16, 32, 64, 128};
+constexpr int kTcGroups[] = {1, 2, 4};
+constexpr int kTcTuneMinPairs = 256;   // smaller plans take the default shape untimed
+constexpr int kTcChunkDefault = 64, kTcGroupDefault = 1;
+
 // Tiles of the tensor-core contraction: the plan's pairs sorted by Jmax
-// (stable), 64 per tile; work items of kTcChunk (m1, m2) combinations; launch
-// groups of at most kTcMaxBuckets bandwidths; the FFT stage's groups of
-// pairs.  Fills pl->tc_meta (tiles, items, FFT groups) and pl->tcb and
-// returns the floats of the sum buffer S.
-static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
+// (stable), 64 per tile (fixed for the plan).  Returns the floats of the sum
+// buffer S.
+static size_t tc_plan_tiles(fo_plan *pl) {
     const int np = pl->npairs;
-    std::vector<int> order(np);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pl->hp[a].L < pl->hp[b].L; });
-    std::vector<fo::TcTile> tiles;
-    std::vector<fo::TcItem> items;
-    std::vector<fo::TcFftGroup> fgroups;
-    size_t fsm = 0;
-    std::vector<int> tile_L;
+    pl->tc_order.resize(np);
+    std::iota(pl->tc_order.begin(), pl->tc_order.end(), 0);
+    std::stable_sort(pl->tc_order.begin(), pl->tc_order.end(),
+                     [&](int a, int b) { return pl->hp[a].L < pl->hp[b].L; });
+    const std::vector<int> &order = pl->tc_order;
+    pl->tc_tiles.clear();
+    pl->tc_tile_t0.clear();
     size_t sfl = 0;
     for (int a = 0; a < np;) {
         const int L = pl->hp[order[a]].L;
@@ -636,26 +660,27 @@ static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
             T.npairs = std::min(fo::kTcTile, b - t0);
             T.s0 = (long long)sfl;
             for (int i = 0; i < T.npairs; ++i) T.coef0[i] = pl->hp[order[t0 + i]].coef0;
-            const int npg = fo::tc_fft_group(G);
-            for (int q0 = 0; q0 < T.npairs; q0 += npg) {
-                fo::TcFftGroup fg{};
-                fg.s0 = (long long)sfl;
-                fg.L = L;
-                fg.ntile = T.npairs;
-                fg.p0 = q0;
-                fg.npg = std::min(npg, T.npairs - q0);
-                for (int q = 0; q < fg.npg; ++q) fg.pair[q] = order[t0 + q0 + q];
-                fgroups.push_back(fg);
-            }
-            fsm = std::max(fsm, fo::tc_fft_smem(G));
             sfl += 2ull * G * W2 * 2 * T.npairs;
-            tiles.push_back(T);
-            tile_L.push_back(L);
+            pl->tc_tiles.push_back(T);
+            pl->tc_tile_t0.push_back(t0);
         }
         a = b;
     }
-    // launch groups over the distinct bandwidths, in increasing order
-    std::vector<int> Ls(tile_L);
+    pl->tc = true;
+    return sfl;
+}
+
+// The work of one tile shape: contraction work items of `chunk` (m1, m2)
+// combinations (launch groups of at most kTcMaxBuckets bandwidths) and FFT
+// blocks of up to `group` pairs.  Fills pl->tc_meta (tiles, items, FFT
+// groups), pl->tcb.launches, ngroups and fft_smem.
+static void tc_plan_shape(fo_ctx *ctx, fo_plan *pl, int chunk, int group) {
+    std::vector<fo::TcTile> tiles = pl->tc_tiles;
+    std::vector<fo::TcItem> items;
+    std::vector<fo::TcFftGroup> fgroups;
+    size_t fsm = 0;
+    std::vector<int> Ls;
+    for (const auto &T : tiles) Ls.push_back(T.L);
     Ls.erase(std::unique(Ls.begin(), Ls.end()), Ls.end());
     pl->tcb.launches.clear();
     for (size_t g0 = 0; g0 < Ls.size(); g0 += fo::kTcMaxBuckets) {
@@ -669,15 +694,30 @@ static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
             lg.maps.nr[bi - g0] = fo::tc_rows(bw);
             lg.nrmax = std::max(lg.nrmax, fo::tc_rows(bw));
             for (size_t t = 0; t < tiles.size(); ++t) {
-                if (tile_L[t] != Ls[bi]) continue;
+                if (tiles[t].L != Ls[bi]) continue;
                 tiles[t].bucket = (int)(bi - g0);
                 const int W2 = (2 * Ls[bi] + 1) * (2 * Ls[bi] + 1);
-                for (int m0 = 0; m0 < W2; m0 += fo::kTcChunk)
-                    items.push_back(fo::TcItem{(int)t, m0, std::min(W2, m0 + fo::kTcChunk), 0});
+                for (int m0 = 0; m0 < W2; m0 += chunk)
+                    items.push_back(fo::TcItem{(int)t, m0, std::min(W2, m0 + chunk), 0});
             }
         }
         lg.nitems = (int)items.size() - lg.item0;
         pl->tcb.launches.push_back(lg);
+    }
+    for (size_t t = 0; t < tiles.size(); ++t) {
+        const fo::TcTile &T = tiles[t];
+        const int G = 2 * (T.L + 1), npg = fo::tc_fft_group(G, group);
+        for (int q0 = 0; q0 < T.npairs; q0 += npg) {
+            fo::TcFftGroup fg{};
+            fg.s0 = T.s0;
+            fg.L = T.L;
+            fg.ntile = T.npairs;
+            fg.p0 = q0;
+            fg.npg = std::min(npg, T.npairs - q0);
+            for (int q = 0; q < fg.npg; ++q) fg.pair[q] = pl->tc_order[pl->tc_tile_t0[t] + q0 + q];
+            fgroups.push_back(fg);
+        }
+        fsm = std::max(fsm, fo::tc_fft_smem(G, npg));
     }
     const size_t bt = tiles.size() * sizeof(fo::TcTile);
     pl->tc_off_items = align256(bt);
@@ -688,8 +728,99 @@ static size_t tc_plan_layout(fo_ctx *ctx, fo_plan *pl) {
     memcpy(pl->tc_meta.data() + pl->tc_off_groups, fgroups.data(), fgroups.size() * sizeof(fo::TcFftGroup));
     pl->tcb.ngroups = (int)fgroups.size();
     pl->tcb.fft_smem = fsm;
-    pl->tc = true;
-    return sfl;
+    pl->tc_chunk = chunk;
+    pl->tc_group = group;
+}
+
+// Device bytes of the tile metadata for the largest shape the autotuner tries.
+static size_t tc_meta_capacity(fo_ctx *ctx, fo_plan *pl) {
+    tc_plan_shape(ctx, pl, kTcChunks[0], 1);   // most items, most FFT groups
+    return pl->tc_meta.size();
+}
+
+static fo_status tc_status(fo_plan *pl);
+
+// Upload the tile metadata of the current shape and point the kernels at it.
+static fo_status tc_upload_meta(fo_plan *pl) {
+    fo::TcBuffers &t = pl->tcb;
+    unsigned char *mb = pl->tc_meta_dev;
+    t.tiles = (const fo::TcTile *)mb;
+    t.items = (const fo::TcItem *)(mb + pl->tc_off_items);
+    t.groups = (const fo::TcFftGroup *)(mb + pl->tc_off_groups);
+    cudaMemcpyAsync(mb, pl->tc_meta.data(), pl->tc_meta.size(), cudaMemcpyHostToDevice, pl->ctx->stream);
+    return cuda_check(pl->ctx, cudaStreamSynchronize(pl->ctx->stream), "tile metadata");
+}
+
+// The plan-shape key of the autotuner: the plan's distinct Jmax values and its
+// pair count rounded up to a power of two.
+static std::string tc_shape_key(const fo_plan *pl) {
+    std::string k;
+    int last = -1;
+    for (const auto &T : pl->tc_tiles)
+        if (T.L != last) { k += std::to_string(T.L) + ","; last = T.L; }
+    int p2 = 1;
+    while (p2 < pl->npairs) p2 *= 2;
+    return k + "n" + std::to_string(p2);
+}
+
+// Pick the tensor-core tile shape of a plan.  Autotuner: for a plan shape
+// not seen before (at least kTcTuneMinPairs pairs), compute the plan's
+// coefficients once, then time the contraction and the FFT stage for every
+// (chunk, group) of kTcChunks x kTcGroups with CUDA events (best of two
+// runs each) and keep the fastest for this context; later plans of the same
+// shape reuse it.  Smaller plans, and contexts with autotuning off, take the
+// default shape.
+static fo_status tc_tune(fo_ctx *ctx, fo_plan *pl) {
+    int chunk = kTcChunkDefault, group = kTcGroupDefault;
+    const std::string key = tc_shape_key(pl);
+    bool tune = ctx->autotune && pl->npairs >= kTcTuneMinPairs;
+    auto it = ctx->tc_shapes.find(key);
+    if (it != ctx->tc_shapes.end()) {
+        chunk = it->second.first;
+        group = it->second.second;
+        tune = false;
+    }
+    if (tune) {
+        cudaStream_t st = ctx->stream;
+        cudaMemsetAsync(pl->d_coef, 0, pl->coef_bytes, st);
+        fo::launch_sph_center(pl->sb, st);
+        fo::launch_sph_ylm(pl->sb, pl->fp32, st);
+        fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
+        fo::launch_sph_coeff(pl->sb, pl->fp32, st);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = 3.0e38f;
+        fo_status s = FO_OK;
+        for (int c : kTcChunks)
+            for (int g : kTcGroups) {
+                tc_plan_shape(ctx, pl, c, g);
+                s = tc_upload_meta(pl);
+                if (s) break;
+                float t = 3.0e38f;
+                for (int rep = 0; rep < 2; ++rep) {
+                    cudaMemsetAsync(pl->tcb.err, 0, sizeof(int), st);
+                    cudaEventRecord(e0, st);
+                    fo::launch_wigner_tc(pl->tcb, st);
+                    fo::launch_isoft_tc(pl->tcb, st);
+                    cudaEventRecord(e1, st);
+                    s = cuda_check(ctx, cudaEventSynchronize(e1), "tile-shape timing");
+                    if (!s) s = tc_status(pl);
+                    if (s) break;
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    t = std::min(t, ms);
+                }
+                if (s) break;
+                if (t < best) { best = t; chunk = c; group = g; }
+            }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (s) return s;
+        ctx->tc_shapes[key] = {chunk, group};
+    }
+    tc_plan_shape(ctx, pl, chunk, group);
+    return tc_upload_meta(pl);
 }
 
 // harm_n < 0: the Gaussian-kernel coefficients of ALIGN; harm_n >= 0: the
@@ -806,19 +937,25 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
     bws.erase(std::unique(bws.begin(), bws.end()), bws.end());
     fo_status s = ensure_dtabs(ctx, bws);
     if (s) { delete pl; return s; }
-    size_t tc_s = 0;
+    size_t tc_s = 0, tc_meta_cap = 0;
     if (pl->fp32 && ctx->tc) {
         s = ensure_tc_tables(ctx, bws);
         if (s) { delete pl; return s; }
-        tc_s = tc_plan_layout(ctx, pl);
+        tc_s = tc_plan_tiles(pl);
+        tc_meta_cap = tc_meta_capacity(ctx, pl);
     }
     build_buckets(pl, rassign, cand_list);
     pl->harm_n = harm_n >= 0 ? harm_n : -1;
     pl->harm_d = harm_n >= 0 ? 2 * (size_t)pl->nslots * (harm_n + 1) * (pl->maxL + 1) : 0;
     s = plan_common_alloc(ctx, pl, contig ? pos1 : hpos1.data(), contig ? pos2 : hpos2.data(), slot2orig,
                           slot2pair, cand2pair, cand_list, ylm_n, w_n, coef_n, grid_n, 0, lap_total,
-                          pl->tc_meta.size(), tc_s);
+                          tc_meta_cap, tc_s);
     if (s) { fo_plan_destroy(pl); return s; }
+    if (pl->tc) {
+        pl->sb.dtab = (const void *const *)ctx->d_dtab32;
+        s = tc_tune(ctx, pl);
+        if (s) { fo_plan_destroy(pl); return s; }
+    }
     pl->sb.dtab = pl->fp32 ? (const void *const *)ctx->d_dtab32 : (const void *const *)ctx->d_dtab64;
     *out = pl;
     return FO_OK;

@@ -130,13 +130,12 @@ struct TcTile {
     long long coef0[kTcTile];   // complex offset of each pair's coefficients (ilmm layout)
 };
 struct TcItem { int tile, mm0, mm1, pad; };
-// Pairs per block of the FFT stage (G <= 32; always one when G = 64).  One
-// pair per block measured faster than four at 4096 pairs (2.06 vs 2.21 ms).
-#ifndef FO_TC_FFT_GROUP
-#define FO_TC_FFT_GROUP 1
-#endif
-constexpr int kTcFftGroup = FO_TC_FFT_GROUP;
-__host__ __device__ inline int tc_fft_group(int G) { return G <= 32 ? kTcFftGroup : 1; }
+// Pairs per block of the FFT stage: at most kTcFftGroup, one when G = 64
+// (the autotuner picks the group size per plan shape).
+constexpr int kTcFftGroup = 4;
+__host__ __device__ inline int tc_fft_group(int G, int group) {
+    return G <= 32 ? (group < kTcFftGroup ? group : kTcFftGroup) : 1;
+}
 struct TcFftGroup {
     long long s0;   // its tile's S offset
     int L;          // Jmax of the tile
@@ -173,7 +172,7 @@ size_t tc_table_floats(int bw);      // floats of its table
 bool tc_make_table(int bw, const double *d64, float *out, CUtensorMap *map, cudaStream_t s);
 void launch_wigner_tc(const TcBuffers &b, cudaStream_t s);   // the contraction (tcgen05)
 void launch_isoft_tc(const TcBuffers &b, cudaStream_t s);    // the FFT stage after it
-size_t tc_fft_smem(int G);           // its dynamic shared memory for planes of edge G
+size_t tc_fft_smem(int G, int npg);  // its dynamic shared memory: npg pairs of planes of edge G
 
 // context options (library-internal; the server creates worker contexts)
 fo_opts ctx_opts(const fo_ctx *ctx);

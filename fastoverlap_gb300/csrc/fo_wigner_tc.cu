@@ -473,7 +473,7 @@ void launch_wigner_tc(const TcBuffers &b, cudaStream_t s) {
     }
 }
 
-size_t tc_fft_smem(int G) { return sizeof(float2) * (3ull * tc_fft_group(G) * isoft_plane(G) + G); }
+size_t tc_fft_smem(int G, int npg) { return sizeof(float2) * (3ull * npg * isoft_plane(G) + G); }
 
 void launch_isoft_tc(const TcBuffers &b, cudaStream_t s) {
     allow_max_smem<k_isoft_tc>();

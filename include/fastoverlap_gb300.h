@@ -128,6 +128,15 @@ fo_status   fo_set_precision(fo_ctx *ctx, int precision);
  * cores in split TF32 (3xTF32, FP32 accumulation); 0 on the FP32 CUDA cores.
  * Applies to plans created afterwards; the FP64 form never uses it.          */
 fo_status   fo_set_tensor_cores(fo_ctx *ctx, int on);
+/* No counterpart in the reference.  1 (default): a mixed-form plan of at
+ * least 256 pairs whose shape (distinct Jmax values, pair count rounded up
+ * to a power of two) this context has not seen picks its tensor-core tile
+ * shape -- (m1, m2) combinations per contraction CTA in {16, 32, 64, 128},
+ * pairs per FFT block in {1, 2, 4} -- by timing every shape once at plan
+ * creation; the choice is kept in the context for later plans of the shape.
+ * 0: the default shape (64, 1).  fo_plan_tile_shape reports a plan's shape
+ * (0, 0 when it does not use the tensor cores).                             */
+fo_status   fo_set_autotune(fo_ctx *ctx, int on);
 
 /* ---- batched entry points (host buffers in, host buffers out) ----
  * pos1 = target structures (COORDSB), pos2 = structures moved onto them
@@ -197,6 +206,7 @@ fo_status fo_plan_wait(fo_plan *plan);
 fo_status fo_plan_results(fo_plan *plan, double *aligned, int *permbest,
                           fo_pair_result *results);
 size_t    fo_plan_device_bytes(const fo_plan *plan);
+fo_status fo_plan_tile_shape(const fo_plan *plan, int *chunk, int *group);
 int       fo_plan_launches(const fo_plan *plan);   /* kernel launches per fo_plan_run */
 void      fo_plan_destroy(fo_plan *plan);
 
