@@ -13,9 +13,11 @@ pass of the whole alignment pipeline over the batch.
   config: also reports the plain FP64 GPU form (batched and one pair per
           call), the error of the mixed form against FP64, the large-bandwidth
           study (config.precision_study_c3: 64 pairs of 1000 atoms at Jmax 31,
-          FP64 against mixed), and a served
-          stream (config.serving): Poisson arrivals (70% spherical N 13..500,
-          30% periodic N 64..1024) through fo_server_* with p50/p99 latency.
+          FP64 against mixed), and a served stream (config.serving, 2000
+          req/s for 60 s): Poisson arrivals (70% spherical N 13..500, 30%
+          periodic N 64..1024) through fo_server_* with p50/p99 latency and
+          the median latency per 10 s window; config.serving_fp64 serves the
+          same stream in plain FP64 at a rate near its capacity.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--npairs P] [--precision mixed|fp64]
@@ -29,6 +31,7 @@ import argparse
 import json
 import multiprocessing as mp
 import os
+import queue
 import statistics
 import subprocess
 import sys
@@ -154,26 +157,49 @@ def serve_run(rate, duration, precision, workers=2):
         _submit_req(srv, q)
     srv.close()
     srv = Server(precision=precision, workers=workers)
-    tickets = []
+    # a second thread collects the tickets in submission order while the
+    # stream runs; the time a ticket is collected bounds its completion from
+    # above, which is enough to show whether latency grows over the run
+    todo = queue.Queue()
+    done = []
+
+    def collect():
+        while True:
+            item = todo.get()
+            if item is None:
+                return
+            t, ts = item
+            srv.wait(t)
+            done.append((ts, time.time() - t0 - ts))
+
     t0 = time.time()
+    waiter = threading.Thread(target=collect)
+    waiter.start()
     for ta, q in reqs:
         dt = t0 + ta - time.time()
         if dt > 0:
             time.sleep(dt)
-        tickets.append(_submit_req(srv, q))
+        todo.put((_submit_req(srv, q), time.time() - t0))
     t_sub = time.time() - t0
-    for t in tickets:
-        srv.wait(t)
+    todo.put(None)
+    waiter.join()
     wall = time.time() - t0
     st = srv.stats()
     srv.close()
     ncl = sum(1 for _, q in reqs if q["kind"] == "cluster")
+    win = 10.0 if duration >= 20 else max(duration / 2.0, 1e-3)
+    by_win = []
+    for w0 in np.arange(0.0, t_sub, win):
+        lat = [l for ts, l in done if w0 <= ts < w0 + win]
+        if lat:
+            by_win.append(round(1e3 * float(np.median(lat)), 1))
     return {"arrival_rate_per_s": rate, "duration_s": duration, "requests": len(reqs),
             "spherical": ncl, "periodic": len(reqs) - ncl, "submit_s": t_sub, "wall_s": wall,
             "workers": workers, "completed_per_s": st["completed"] / wall, "failed": int(st["failed"]),
             "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
             "latency_max_ms": st["latency_max_ms"], "batches": int(st["batches"]),
             "mean_batch": st["mean_batch"],
+            "collected_p50_ms_by_window": by_win, "window_s": win,
             "stand_in": "requests drawn from 48 spherical + 16 periodic seeded base structures, "
                         "each with a fresh rotation/translation, permutation and noise"}
 
@@ -344,7 +370,10 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=32)
     ap.add_argument("--c3-pairs", type=int, default=64, help="0 skips the large-bandwidth study")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
-    ap.add_argument("--serve-duration", type=float, default=5.0, help="0 skips the served stream")
+    ap.add_argument("--serve-duration", type=float, default=60.0, help="0 skips the served stream")
+    ap.add_argument("--serve-fp64-rate", type=float, default=200.0,
+                    help="arrival rate of the plain FP64 served stream (its capacity is far lower)")
+    ap.add_argument("--serve-fp64-duration", type=float, default=10.0, help="0 skips the FP64 served stream")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -499,6 +528,10 @@ def main():
             "kernel_ms_per_launch": top_ms,
             "kernel_share": kern[top][0] / sum(v[0] for v in kern.values())}
     launches = batch.plan_launches() * args.steps
+    chunk, group = batch.plan_tile_shape()
+    if chunk:
+        cfg_extra["tc_tile_shape"] = {"wigner_pairs_per_chunk": chunk, "fft_pairs_per_block": group,
+                                      "picked_by": "autotuner (timed per plan shape, cached per context)"}
 
     if args.c3_pairs > 0:
         try:
@@ -511,6 +544,15 @@ def main():
             cfg_extra["serving"] = serve_run(args.serve_rate, args.serve_duration, args.precision)
         except Exception as e:   # reported, never required
             cfg_extra["serving"] = {"error": str(e)}
+    if args.serve_fp64_duration > 0 and args.precision == "mixed":
+        try:
+            sv = serve_run(args.serve_fp64_rate, args.serve_fp64_duration, "fp64")
+            cfg_extra["serving_fp64"] = sv
+            if "completed_per_s" in cfg_extra.get("serving", {}):
+                cfg_extra["serving_mixed_over_fp64_completed"] = (cfg_extra["serving"]["completed_per_s"] /
+                                                                   sv["completed_per_s"])
+        except Exception as e:   # reported, never required
+            cfg_extra["serving_fp64"] = {"error": str(e)}
 
     cpu = None
     if not args.no_cpu_baseline:
