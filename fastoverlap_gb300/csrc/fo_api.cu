@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -255,6 +256,12 @@ fo_status finish_plan_alloc(fo_ctx *ctx, fo_plan *pl, size_t bytes) {
     return FO_OK;
 }
 
+// 1: buckets of the mixed form with groups of more than 256 atoms run
+// multi-warp blocks (helper warps for the neighbour lists)
+#ifndef FO_REFINE_MW
+#define FO_REFINE_MW 1
+#endif
+
 constexpr size_t kRefSmemCap = 96 * 1024;     // assignment arrays kept on chip up to this size
 constexpr size_t kRefSplitCap = 120 * 1024;   // above it: only the working arrays on chip, up to this
 
@@ -263,6 +270,7 @@ struct RefAssign {
     long long lapstride;
     int ct64;
     int split;   // working arrays on chip, costs / neighbour lists in global scratch
+    int mw;      // mixed form with groups for the multi-warp neighbour lists
 };
 
 // Shared-memory footprint of one refinement warp for a pair, and whether its
@@ -272,6 +280,7 @@ struct RefAssign {
 RefAssign ref_assign(int n, int maxg, bool fp32, bool recomp, double dmax) {
     RefAssign r;
     r.ct64 = (dmax * dmax * fo::kPScale >= 2.0e9) ? 1 : 0;
+    r.mw = (fp32 && recomp && fo::ref_multiwarp(maxg)) ? 1 : 0;
     fo::RefLayout L;
     fo::ref_layout(n, maxg, fp32, r.ct64 ? 8 : 4, recomp, L);
     // Footprint classes, one launch each: the largest dynamic shared memory
@@ -313,10 +322,11 @@ void build_buckets(fo_plan *pl, const std::vector<RefAssign> &ra, std::vector<in
     std::vector<int> order(pl->hp.size());
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pl->hp[a].n > pl->hp[b].n; });
-    std::map<std::pair<int, size_t>, std::vector<int>> by;
+    // key: (footprint, 64-bit costs, multi-warp neighbour lists)
+    std::map<std::tuple<size_t, int, int>, std::vector<int>> by;
     for (int i : order) {
         const fo::PairDev &P = pl->hp[i];
-        auto &v = by[{ra[i].ct64, ra[i].smem}];
+        auto &v = by[{ra[i].smem, ra[i].ct64, ra[i].mw}];
         for (int c = 0; c < P.norient * P.nrot; ++c) v.push_back(P.cand0 + c);
     }
     pl->buckets.clear();
@@ -328,8 +338,9 @@ void build_buckets(fo_plan *pl, const std::vector<RefAssign> &ra, std::vector<in
         fo::RefineBucket b;
         b.offset = (int)cand_list.size();
         b.count = (int)kv.second.size();
-        b.smem = kv.first.second;
-        b.ct64 = kv.first.first;
+        b.smem = std::get<0>(kv.first);
+        b.ct64 = std::get<1>(kv.first);
+        b.nw = (std::get<2>(kv.first) && FO_REFINE_MW) ? fo::refine_block_warps(pl->bulk, b.ct64, b.smem) : 1;
         cand_list.insert(cand_list.end(), kv.second.begin(), kv.second.end());
         pl->buckets.push_back(b);
     }

@@ -78,9 +78,11 @@ void launch_bulk_fft(const BulkBuffers &b, bool fp32, cudaStream_t s);
 // peaks and refinement (shared)
 struct RefineBucket {
     int offset, count;  // slice of cand_list
-    size_t smem;        // dynamic shared memory per candidate (one warp)
+    size_t smem;        // dynamic shared memory per candidate
     int ct64;           // 64-bit integer costs
+    int nw;             // warps per candidate (> 1: helpers for the neighbour lists, mixed form)
 };
+int refine_block_warps(bool bulk, bool ct64, size_t smem);
 
 struct RefineBuffers {
     const PairDev *pairs;

@@ -951,15 +951,15 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
 // Rows of up to 32*kNearReg columns keep their distances in registers.
 constexpr int kNearReg = 16;
 
-template <typename KT, typename DF>
+template <typename KT, int NR, typename DF>
 __device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, const DF &dist, float *thr = nullptr,
                              bool warm = false) {
     const int lane = threadIdx.x & 31;
     const unsigned ltmask = (1u << lane) - 1u;
-    const bool inreg = ns <= 32 * kNearReg;
-    unsigned r[kNearReg];   // bit patterns of columns lane + 32k (all ones beyond ns)
+    const bool inreg = ns <= 32 * NR;
+    unsigned r[NR];   // bit patterns of columns lane + 32k (all ones beyond ns)
 #pragma unroll
-    for (int k = 0; k < kNearReg; ++k) {
+    for (int k = 0; k < NR; ++k) {
         const int j = lane + 32 * k;
         r[k] = (inreg && j < ns) ? __float_as_uint(dist(j)) : 0xffffffffu;
     }
@@ -970,7 +970,7 @@ __device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, cons
         int c = 0;
         if (inreg) {
 #pragma unroll
-            for (int k = 0; k < kNearReg; ++k) c += r[k] < t;
+            for (int k = 0; k < NR; ++k) c += r[k] < t;
         } else {
             for (int j = lane; j < ns; j += 32) c += __float_as_uint(d[j]) < t;
         }
@@ -1010,7 +1010,7 @@ __device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, cons
         unsigned u = 0xffffffffu;
         if (inreg) {
 #pragma unroll
-            for (int k = 0; k < kNearReg; ++k)
+            for (int k = 0; k < NR; ++k)
                 if (b0 == 32 * k) u = r[k];
         } else if (j < ns) {
             u = __float_as_uint(d[j]);
@@ -1023,6 +1023,48 @@ __device__ void nearest_warp(KT *krow, float *d, const int ns, const int m, cons
         need_eq -= min(need_eq, __popc(em));
     }
     __syncwarp();
+}
+
+// Neighbour-list work of one group handed from the first warp of a
+// multi-warp block to the others (shared memory; mixed form).
+struct NbrCmd {
+    int op;                  // 1: rows of this group; 0: the candidate is done
+    int ns, m, warm;
+    const float4 *b4, *a4;   // the group's FP32 coordinates
+    void *kk;                // its neighbour lists (ns rows of m)
+    float *thr;              // its rows' last m-th distances
+    float bx[3], rx[3];      // box lengths and reciprocals (0: no wrap)
+};
+
+__device__ __forceinline__ void named_bar(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Rows w, w + nw, ... of the group in cmd, one row per warp at a time.
+template <typename KT, bool BOX>
+__device__ void nbr_rows(const NbrCmd &cmd, int w, int nw) {
+    const CostF32<int, BOX> cf{cmd.b4, cmd.a4, {cmd.bx[0], cmd.bx[1], cmd.bx[2]}, {cmd.rx[0], cmd.rx[1], cmd.rx[2]}};
+    KT *kk = (KT *)cmd.kk;
+    for (int i = w; i < cmd.ns; i += nw)
+        nearest_warp<KT, kNearRegMW>(kk + (size_t)i * cmd.m, nullptr, cmd.ns, cmd.m, [&](int j) { return cf.d2(i, j); },
+                                     cmd.thr + i, cmd.warm != 0);
+}
+
+// The warps after the first of a multi-warp block: wait for neighbour-list
+// work (barrier 1), do their rows, report them done (barrier 2), until the
+// first warp posts op 0.  The first warp passes barrier 1 exactly once per
+// command it posts and once more with op 0 before it finishes the candidate.
+template <bool BOX>
+__device__ void nbr_helper(volatile NbrCmd *cmdv, int kkbytes) {
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (;;) {
+        named_bar(1, blockDim.x);
+        if (cmdv->op == 0) return;
+        const NbrCmd &cmd = *(const NbrCmd *)cmdv;
+        if (kkbytes == 1) nbr_rows<uint8_t, BOX>(cmd, w, nw);
+        else nbr_rows<uint16_t, BOX>(cmd, w, nw);
+        named_bar(2, blockDim.x);
+    }
 }
 
 // Coordinates of one permutation group as the assignment sees them: rows are
@@ -1045,7 +1087,7 @@ struct GroupCoords {
 // JOVOSAP for one group).  Returns the assignment's status.
 template <typename KT, typename DT, typename CT, bool RECOMP, bool BOX>
 __device__ int assign_group(const int ns, const int m, const GroupCoords &G, unsigned char *lb, unsigned char *lbk,
-                            const RefLayout &L, float *thr = nullptr, bool warm = false) {
+                            const RefLayout &L, float *thr = nullptr, bool warm = false, NbrCmd *cmd = nullptr) {
     const int lane = threadIdx.x & 31;
     const bool dense = (m == ns);
     constexpr bool kF32 = sizeof(DT) == 4;   // mixed form: no augmenting row reduction
@@ -1061,11 +1103,28 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                     float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
                     for (int i = lane; i < ns; i += 32)
                         nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
+                } else if (cmd && thr && ns <= 32 * kNearRegMW) {
+                    // every warp of the block on its own rows (the first warp is the caller)
+                    if (lane == 0) {
+                        cmd->op = 1;
+                        cmd->ns = ns;
+                        cmd->m = m;
+                        cmd->warm = warm ? 1 : 0;
+                        cmd->b4 = cf.b;
+                        cmd->a4 = cf.a;
+                        cmd->kk = kk;
+                        cmd->thr = thr;
+                        for (int k = 0; k < 3; ++k) { cmd->bx[k] = cf.bx[k]; cmd->rx[k] = cf.rx[k]; }
+                    }
+                    __syncwarp();
+                    named_bar(1, blockDim.x);
+                    nbr_rows<KT, BOX>(*cmd, 0, blockDim.x >> 5);
+                    named_bar(2, blockDim.x);
                 } else {   // the warp on one row at a time, from the row's last m-th distance when warm
                     float *dr = (float *)(lb + L.lap_heap);
                     for (int i = 0; i < ns; ++i)
-                        nearest_warp<KT>(kk + i * m, dr, ns, m, [&](int j) { return cf.d2(i, j); },
-                                         thr ? thr + i : nullptr, warm);
+                        nearest_warp<KT, kNearReg>(kk + i * m, dr, ns, m, [&](int j) { return cf.d2(i, j); },
+                                                   thr ? thr + i : nullptr, warm);
                 }
             }
             __syncwarp();
@@ -1135,15 +1194,22 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
 // the candidate's output slot (cxyz); the fixed structure and the rotated
 // starting structure are recomputed from the inputs where they are read, with
 // the same expressions as when they are first formed.
-template <typename DT, typename CT, bool RECOMP, bool BOX>
-__global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
-    const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
-    const double *xa, const double *xb, const double *peaks, const int *npeaks, unsigned char *lapg,
-    double *cdist, double *cR, double *cdisp, double *cxyz, int *cperm, int *cniter, int *cstat, float *cthr) {
+// MW: blocks of up to kRefMaxWarps warps (mixed form, groups of more than
+// kHeapMaxRow atoms): the first warp runs the candidate, the others help with
+// its neighbour lists.  The register budget per thread equals the one-warp
+// kernel's (FO_REFINE_MINB one-warp blocks per SM).
+template <typename DT, typename CT, bool RECOMP, bool BOX, bool MW = false>
+__global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MINB / kRefMaxWarps : FO_REFINE_MINB)
+    k_refine_warp(const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
+                  const double *xa, const double *xb, const double *peaks, const int *npeaks, unsigned char *lapg,
+                  double *cdist, double *cR, double *cdisp, double *cxyz, int *cperm, int *cniter, int *cstat,
+                  float *cthr) {
     constexpr bool kF32 = sizeof(DT) == 4;
     static_assert(kF32 || !RECOMP, "costs are recomputed only from FP32 coordinates");
+    static_assert(!MW || (kF32 && RECOMP), "helper warps serve the mixed form's neighbour lists only");
     extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x;
+    __shared__ NbrCmd scmd;
+    const int lane = threadIdx.x & 31;
     const int c = cand_list[blockIdx.x];
     const int p = cand2pair[c];
     const PairDev &P = pairs[p];
@@ -1174,6 +1240,13 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
         // from few FP64 instructions (Horn rotation, one affine map per step).
         __shared__ double sRb[9], sRn[9], sRc[9], sRs[9], sT[12], sF[8];
         float *thrc = cthr + ob;   // per row: its m-th neighbour distance in the last iteration
+        if constexpr (MW) {
+            if (threadIdx.x >= 32) {   // helper warps: neighbour-list rows until the first warp is done
+                nbr_helper<BOX>(&scmd, L.kkbytes);
+                return;
+            }
+        }
+        NbrCmd *cmd = MW ? &scmd : nullptr;
         GroupCoords GC;
         GC.bulk = bulk;
         GC.xb = XB;
@@ -1308,8 +1381,8 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
                 GC.A = DA + 3 * s0;
                 GC.B4 = B4 + s0;
                 GC.A4 = A4 + s0;
-                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0)
-                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0);
+                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0, cmd)
+                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0, cmd);
                 if (rc) fail += 1;
                 __syncwarp();
                 for (int i = lane; i < ns; i += 32) {
@@ -1437,6 +1510,12 @@ __global__ void __launch_bounds__(32, FO_REFINE_MINB) k_refine_warp(
             for (int k = 0; k < 3; ++k) cdisp[3LL * c + k] = db[k] - d0[k];
             cniter[c] = ntries;
             cstat[c] = fail ? (int)ST_LAP_FAILED : 0;
+        }
+        if constexpr (MW) {   // release the helper warps
+            __syncwarp();
+            if (lane == 0) scmd.op = 0;
+            __syncwarp();
+            named_bar(1, blockDim.x);
         }
     } else {
         __shared__ double sRb[9], sRn[9], sRc[9];
@@ -1745,6 +1824,31 @@ __global__ void k_select(const PairDev *pairs, const int *slot2orig, const int *
 }
 
 
+// Warps per block for a bucket of the mixed form whose groups take the
+// multi-warp neighbour lists: as many as the register file holds next to the
+// blocks that the shared-memory footprint already lets share an SM (at most
+// kRefMaxWarps; 1 when the footprint allows many blocks anyway).
+int refine_block_warps(bool bulk, bool ct64, size_t smem) {
+    const void *fn = bulk ? (ct64 ? (const void *)k_refine_warp<float, long long, true, true, true>
+                                  : (const void *)k_refine_warp<float, int, true, true, true>)
+                          : (ct64 ? (const void *)k_refine_warp<float, long long, true, false, true>
+                                  : (const void *)k_refine_warp<float, int, true, false, true>);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) { cudaGetLastError(); return 1; }
+    int dev = 0, smsm = 0, regsm = 0, thrsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&regsm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&thrsm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    const size_t per_block = smem + fa.sharedSizeBytes + 1024;
+    const int blocks = per_block ? (int)((size_t)smsm / per_block) : 0;
+    if (blocks < 1 || blocks >= FO_REFINE_MINB / 2) return 1;
+    const int regs = fa.numRegs > 0 ? fa.numRegs : 128;
+    int nw = regsm / (blocks * 32 * regs);
+    nw = min(nw, thrsm / (blocks * 32));
+    return max(1, min(nw, kRefMaxWarps));
+}
+
 // Buckets run concurrently on the auxiliary streams (fork/join through
 // events on the main stream) so that small and large problems share the SMs.
 void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,
@@ -1763,7 +1867,22 @@ void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux,
             b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,      \
             b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat, b.cthr);                               \
     } while (0)
-        if (b.fp32 && b.recomp) {
+#define FO_LAUNCH_REFINE_MW(CT, BX)                                                                   \
+    do {                                                                                              \
+        allow_max_smem<k_refine_warp<float, CT, true, BX, true>>();                                  \
+        k_refine_warp<float, CT, true, BX, true><<<bk.count, 32 * bk.nw, bk.smem, s>>>(               \
+            b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,      \
+            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat, b.cthr);                               \
+    } while (0)
+        if (b.fp32 && b.recomp && bk.nw > 1) {
+            if (b.bulk) {
+                if (bk.ct64) FO_LAUNCH_REFINE_MW(long long, true);
+                else FO_LAUNCH_REFINE_MW(int, true);
+            } else {
+                if (bk.ct64) FO_LAUNCH_REFINE_MW(long long, false);
+                else FO_LAUNCH_REFINE_MW(int, false);
+            }
+        } else if (b.fp32 && b.recomp) {
             if (b.bulk) {
                 if (bk.ct64) FO_LAUNCH_REFINE(float, long long, true, true);
                 else FO_LAUNCH_REFINE(float, int, true, true);
@@ -1779,6 +1898,7 @@ void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux,
             else FO_LAUNCH_REFINE(double, int, false, false);
         }
 #undef FO_LAUNCH_REFINE
+#undef FO_LAUNCH_REFINE_MW
     }
     for (int a = 0; a < naux; ++a) {
         cudaEventRecord(join[a], aux[a]);

@@ -19,6 +19,17 @@ struct RefLayout {
 constexpr int kHeapMaxRow = 256;
 constexpr int kHeapStride = 61;
 
+// Mixed form, groups of more than kHeapMaxRow atoms: blocks of up to
+// kRefMaxWarps warps per candidate, where the warps beyond the first only
+// help with the neighbour lists (one row per warp at a time, the row's
+// distances in registers: at most 32 * kNearRegMW columns).  The rest of the
+// refinement stays on the first warp.
+constexpr int kRefMaxWarps = 8;
+constexpr int kNearRegMW = 32;
+__host__ __device__ inline bool ref_multiwarp(int maxg) {
+    return maxg > kHeapMaxRow && maxg <= 32 * kNearRegMW;
+}
+
 __host__ __device__ inline size_t ref_a16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 // Column indices of the neighbour lists fit one byte when no group has more
