@@ -797,12 +797,15 @@ static fo_status tc_tune(fo_ctx *ctx, fo_plan *pl) {
         fo::launch_sph_center(pl->sb, st);
         fo::launch_sph_ylm(pl->sb, pl->fp32, st);
         fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
-        fo::launch_sph_coeff(pl->sb, pl->fp32, st);
+        cudaMemsetAsync(pl->tcb.err, 0, sizeof(int), st);
+        fo::launch_coef_tc(pl->sb, pl->tcb.err, st);
+        fo_status s = cuda_check(ctx, cudaStreamSynchronize(st), "coefficients");
+        if (!s) s = tc_status(pl);
+        if (s) return s;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         float best = 3.0e38f;
-        fo_status s = FO_OK;
         for (int c : kTcChunks)
             for (int g : kTcGroups) {
                 tc_plan_shape(ctx, pl, c, g);
@@ -964,6 +967,7 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
     if (s) { fo_plan_destroy(pl); return s; }
     if (pl->tc) {
         pl->sb.dtab = (const void *const *)ctx->d_dtab32;
+        pl->sb.tc_layout = true;
         s = tc_tune(ctx, pl);
         if (s) { fo_plan_destroy(pl); return s; }
     }
@@ -1101,18 +1105,24 @@ static fo_status tc_status(fo_plan *pl) {
     int terr = 0;
     fo_status s = cuda_check(pl->ctx, cudaMemcpy(&terr, pl->tcb.err, sizeof(int), cudaMemcpyDeviceToHost), "status");
     if (s) return s;
-    return terr ? set_err(pl->ctx, FO_ERR_CUDA, "tensor-core Wigner contraction: a pipeline wait timed out") : FO_OK;
+    return terr ? set_err(pl->ctx, FO_ERR_CUDA, "tensor-core contraction (coefficients or Wigner-d): a pipeline wait timed out") : FO_OK;
 }
 
-// The inverse SO(3) transform of a plan's coefficients onto its grids: the
-// tensor-core contraction and its FFT stage, or the fused CUDA-core kernel.
-static void launch_isoft_stage(fo_plan *pl, cudaStream_t st, bool events) {
+// The coefficient contraction of a cluster plan and the inverse SO(3)
+// transform of its coefficients onto its grids: on the tensor cores (the
+// coefficient contraction, the Wigner-d contraction and its FFT stage) or the
+// CUDA-core kernels.
+static void launch_coef_isoft(fo_plan *pl, cudaStream_t st, bool events) {
     if (pl->tc) {
         cudaMemsetAsync(pl->tcb.err, 0, sizeof(int), st);
+        fo::launch_coef_tc(pl->sb, pl->tcb.err, st);
+        if (events) rec_event(pl, K_COEFF);
         fo::launch_wigner_tc(pl->tcb, st);
         if (events) rec_event(pl, K_WTC);
         fo::launch_isoft_tc(pl->tcb, st);
     } else {
+        fo::launch_sph_coeff(pl->sb, pl->fp32, st);
+        if (events) rec_event(pl, K_COEFF);
         fo::launch_isoft(pl->sb, pl->fp32, st);
     }
     if (events) rec_event(pl, K_ISOFT);
@@ -1136,8 +1146,7 @@ static void plan_enqueue(fo_plan *pl, bool events) {
         fo::launch_sph_center(pl->sb, st);     rec_event(pl, K_CENTER);
         fo::launch_sph_ylm(pl->sb, pl->fp32, st); rec_event(pl, K_YLM);
         fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st); rec_event(pl, K_RADIAL);
-        fo::launch_sph_coeff(pl->sb, pl->fp32, st); rec_event(pl, K_COEFF);
-        launch_isoft_stage(pl, st, events);
+        launch_coef_isoft(pl, st, events);
     } else {
         cudaMemsetAsync(pl->d_fgrid, 0, pl->fgrid_bytes, st);
         rec_event(pl, K_MEMSET);
@@ -1397,8 +1406,7 @@ fo_status fo_cluster_overlap(fo_ctx *ctx, const fo_cluster_pair *pair, const dou
     fo::launch_sph_center(pl->sb, st);
     fo::launch_sph_ylm(pl->sb, pl->fp32, st);
     fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
-    fo::launch_sph_coeff(pl->sb, pl->fp32, st);
-    launch_isoft_stage(pl, st, false);
+    launch_coef_isoft(pl, st, false);
     s = cuda_check(ctx, cudaStreamSynchronize(st), "cluster overlap");
     if (!s) s = tc_status(pl);
     const int L = q.jmax, W = 2 * L + 1, G = 2 * (L + 1);
@@ -1754,8 +1762,7 @@ fo_status fo_calc_overlap_matrices(fo_ctx *ctx, const double *coordslist, int na
         fo::launch_sph_center(pl->sb, st);
         fo::launch_sph_ylm(pl->sb, pl->fp32, st);
         fo::launch_sph_radial(pl->sb, pl->fp32, ctx->opts.cutoff, st);
-        fo::launch_sph_coeff(pl->sb, pl->fp32, st);
-        launch_isoft_stage(pl, st, false);
+        launch_coef_isoft(pl, st, false);
         fo::launch_pair_stats(pl->sb, pl->fp32, d_out, st);
         cudaMemcpyAsync(h.data(), d_out, 2 * nb * sizeof(double), cudaMemcpyDeviceToHost, st);
         s = cuda_check(ctx, cudaStreamSynchronize(st), "overlap matrices");

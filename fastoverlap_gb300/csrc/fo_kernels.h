@@ -46,6 +46,8 @@ struct SphBuffers {
     int npairs, ngroups, nslots, maxL, maxG, maxgroup;
     int harm_n = -1;          // >= 0: harmonic-oscillator basis of this order (all pairs)
     double *hd = nullptr;     // its radial overlaps d_nl, FP64 [side][slot][n][l <= maxL]
+    bool tc_layout = false;   // mixed form on the tensor cores: Y_lm as [lm][atom] per pair and
+                              // radial weights as [l][a][b] per group (read by launch_coef_tc)
 };
 
 constexpr int kMaxHarmN = 40;   // largest harmonic order nmax
@@ -56,6 +58,9 @@ void init_sph_tables();   // constant tables of the current device; before the f
 void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s);
 void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s);
 void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s);
+// the same contraction on the tcgen05 tensor cores (FP32 data in 3xTF32, the
+// tc_layout layouts); *err is set when a pipeline wait timed out
+void launch_coef_tc(const SphBuffers &b, int *err, cudaStream_t s);
 void launch_isoft(const SphBuffers &b, bool fp32, cudaStream_t s);
 void launch_pair_stats(const SphBuffers &b, bool fp32, double *out, cudaStream_t s);
 void launch_wigner_table(int bw, double *d64, float *d32, cudaStream_t s);

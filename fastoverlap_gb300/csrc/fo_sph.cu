@@ -101,10 +101,11 @@ template <> __device__ __forceinline__ const float *ylm_tab<float>() { return c_
 
 // Orthonormal Y_lm (Condon-Shortley phase) for l <= L of every slot of both
 // structures; one thread per (slot, side), computed in the precision T of the
-// output.  Output per slot: (L+1)^2 complex values at index l*l + l + m.  An
-// atom at the origin gets theta = 0.  FP64: e^{i m phi} from sincos(m phi);
-// FP32: by repeated multiplication with e^{i phi}.
-template <typename T, typename T2>
+// output.  Output per slot: (L+1)^2 complex values at index l*l + l + m
+// (TL: per pair [lm][atom], atom fastest, the layout of the tensor-core
+// coefficient contraction).  An atom at the origin gets theta = 0.  FP64:
+// e^{i m phi} from sincos(m phi); FP32: by repeated multiplication with e^{i phi}.
+template <typename T, typename T2, bool TL>
 __global__ void k_sph_ylm(const PairDev *pairs, const int *slot2pair, const double *xa,
                           const double *xb, double *ra, double *rb, T2 *ylmA, T2 *ylmB,
                           int nslots) {
@@ -132,7 +133,8 @@ __global__ void k_sph_ylm(const PairDev *pairs, const int *slot2pair, const doub
         }
     }
     const T st = sqrt(ct * ct < T(1) ? T(1) - ct * ct : T(0));
-    T2 *out = (side ? ylmB : ylmA) + P.ylm0 + (long long)(slot - P.atom0) * (L + 1) * (L + 1);
+    const long long ostride = TL ? P.n : 1;   // between consecutive lm
+    T2 *out = (side ? ylmB : ylmA) + P.ylm0 + (long long)(slot - P.atom0) * (TL ? 1 : (L + 1) * (L + 1));
     T pmm = T(0.28209479177387814347);  // 1/sqrt(4 pi)
     T cm = 1, sm = 0;
     for (int m = 0; m <= L; ++m) {
@@ -153,8 +155,8 @@ __global__ void k_sph_ylm(const PairDev *pairs, const int *slot2pair, const doub
             else if (l == m + 1) pl = C[m] * ct * pmm;
             else pl = A[l * kYlmMax + m] * (ct * p1 - B[l * kYlmMax + m] * p2);
             if (l > m) { p2 = p1; p1 = pl; }
-            out[l * l + l + m] = pack2<T2, T>(pl * cm, pl * sm);
-            if (m > 0) out[l * l + l - m] = pack2<T2, T>(sgn * pl * cm, -sgn * pl * sm);
+            out[(l * l + l + m) * ostride] = pack2<T2, T>(pl * cm, pl * sm);
+            if (m > 0) out[(l * l + l - m) * ostride] = pack2<T2, T>(sgn * pl * cm, -sgn * pl * sm);
         }
     }
 }
@@ -170,8 +172,9 @@ __global__ void k_sph_ylm(const PairDev *pairs, const int *slot2pair, const doub
 // the weights (the recurrence is rescaled before it can overflow T: by 1e-250
 // above 1e250 in FP64, by 1e-28 above 1e28 in FP32, which leaves room for a
 // step's growth (2k+1)/x < 1e8 at x >= 1e-6).  The cutoff test is made in
-// FP64 in both precisions.  Layout per group: W[w0 + (l*n + b)*n + a].
-template <typename T>
+// FP64 in both precisions.  Layout per group: W[w0 + (l*n + b)*n + a]
+// (TL: W[w0 + (l*n + a)*n + b], the layout of the tensor-core contraction).
+template <typename T, bool TL>
 __global__ void k_sph_radial(const PairDev *pairs, const GroupDev *groups, const double *ra,
                              const double *rb, T *W, int cutoff) {
     constexpr T kBig = sizeof(T) == 4 ? T(1.0e28) : T(1.0e250);
@@ -180,11 +183,11 @@ __global__ void k_sph_radial(const PairDev *pairs, const GroupDev *groups, const
     const int n = g.n;
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)n * n) return;
-    const int b = (int)(idx / n), a = (int)(idx % n);
+    const int b = TL ? (int)(idx % n) : (int)(idx / n), a = TL ? (int)(idx / n) : (int)(idx % n);
     const PairDev &P = pairs[g.pair];
     const int L = P.L;
     const double r1d = ra[g.slot0 + a], r2d = rb[g.slot0 + b];
-    T *out = W + g.w0 + (long long)b * n + a;
+    T *out = W + g.w0 + idx;
     const long long lstride = (long long)n * n;
     if (cutoff && !(fabs(r1d - r2d) < 4.0 * P.sigma)) {
         for (int l = 0; l <= L; ++l) out[l * lstride] = T(0);
@@ -279,18 +282,19 @@ __global__ void k_harm_dnl(const PairDev *pairs, const int *slot2pair, const dou
 }
 
 // W_l(b, a) of every atom pair of every group, in the precision T of the
-// contraction (same layout as k_sph_radial).
-template <typename T>
+// contraction (same layouts as k_sph_radial).
+template <typename T, bool TL>
 __global__ void k_harm_radial(const PairDev *pairs, const GroupDev *groups, const double *hd, T *W, int nslots,
                               int nmax, int maxL) {
     const GroupDev g = groups[blockIdx.y];
     const int n = g.n;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)n * n) return;
-    const int b = (int)(idx / n), a = (int)(idx % n), L = pairs[g.pair].L, w = maxL + 1;
+    const int b = TL ? (int)(idx % n) : (int)(idx / n), a = TL ? (int)(idx / n) : (int)(idx % n);
+    const int L = pairs[g.pair].L, w = maxL + 1;
     const double *da = hd + (size_t)(g.slot0 + a) * (nmax + 1) * w;
     const double *db = hd + (size_t)(nslots + g.slot0 + b) * (nmax + 1) * w;
-    T *out = W + g.w0 + (long long)b * n + a;
+    T *out = W + g.w0 + idx;
     const long long lstride = (long long)n * n;
     for (int l = 0; l <= L; ++l) {
         double acc = 0;
@@ -515,14 +519,16 @@ void launch_sph_center(const SphBuffers &b, cudaStream_t s) {
 
 void launch_sph_ylm(const SphBuffers &b, bool fp32, cudaStream_t s) {
     int nth = 2 * b.nslots, bs = 128;
-    if (fp32)
-        k_sph_ylm<float, float2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra,
-                                                                   b.rb, (float2 *)b.ylmA,
-                                                                   (float2 *)b.ylmB, b.nslots);
+    const unsigned nb = (nth + bs - 1) / bs;
+    if (fp32 && b.tc_layout)
+        k_sph_ylm<float, float2, true><<<nb, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra, b.rb,
+                                                        (float2 *)b.ylmA, (float2 *)b.ylmB, b.nslots);
+    else if (fp32)
+        k_sph_ylm<float, float2, false><<<nb, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra, b.rb,
+                                                         (float2 *)b.ylmA, (float2 *)b.ylmB, b.nslots);
     else
-        k_sph_ylm<double, double2><<<(nth + bs - 1) / bs, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb,
-                                                                     b.ra, b.rb, (double2 *)b.ylmA,
-                                                                     (double2 *)b.ylmB, b.nslots);
+        k_sph_ylm<double, double2, false><<<nb, bs, 0, s>>>(b.pairs, b.slot2pair, b.xa, b.xb, b.ra, b.rb,
+                                                           (double2 *)b.ylmA, (double2 *)b.ylmB, b.nslots);
 }
 
 void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t s) {
@@ -532,18 +538,23 @@ void launch_sph_radial(const SphBuffers &b, bool fp32, int cutoff, cudaStream_t 
         const int nth = 2 * b.nslots;
         k_harm_dnl<<<(nth + 127) / 128, 128, 0, s>>>(b.pairs, b.slot2pair, b.ra, b.rb, b.hd, b.nslots, b.harm_n,
                                                     b.maxL);
-        if (fp32)
-            k_harm_radial<float><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.hd, (float *)b.W, b.nslots, b.harm_n,
-                                                      b.maxL);
+        if (fp32 && b.tc_layout)
+            k_harm_radial<float, true><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.hd, (float *)b.W, b.nslots,
+                                                            b.harm_n, b.maxL);
+        else if (fp32)
+            k_harm_radial<float, false><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.hd, (float *)b.W, b.nslots,
+                                                             b.harm_n, b.maxL);
         else
-            k_harm_radial<double><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.hd, (double *)b.W, b.nslots,
-                                                       b.harm_n, b.maxL);
+            k_harm_radial<double, false><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.hd, (double *)b.W, b.nslots,
+                                                              b.harm_n, b.maxL);
         return;
     }
-    if (fp32)
-        k_sph_radial<float><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (float *)b.W, cutoff);
+    if (fp32 && b.tc_layout)
+        k_sph_radial<float, true><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (float *)b.W, cutoff);
+    else if (fp32)
+        k_sph_radial<float, false><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (float *)b.W, cutoff);
     else
-        k_sph_radial<double><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (double *)b.W, cutoff);
+        k_sph_radial<double, false><<<grid, 256, 0, s>>>(b.pairs, b.groups, b.ra, b.rb, (double *)b.W, cutoff);
 }
 
 void launch_sph_coeff(const SphBuffers &b, bool fp32, cudaStream_t s) {
