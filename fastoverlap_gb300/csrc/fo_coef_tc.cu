@@ -51,6 +51,7 @@ constexpr int kCtThreads = 288;
 constexpr int kCtTile = 32;          // atoms a per tile (GEMM1 N, GEMM2 K)
 constexpr int kCtK = 32;             // atoms b per GEMM1 stage
 constexpr int kCtB1Bytes = kCtTile * 128;
+constexpr int kCtAUnits = 4;        // A1 staging units per producer thread: (2l+1) rows x 8 chunks <= 4 x 128
 constexpr int kCtCols = 256;         // tensor memory per CTA
 constexpr int kD2 = 0, kD1 = 128, kH = 192, kLo = 224;   // columns: D2 (<= 128), D1 [2] (32 each), P hi, P lo
 
@@ -157,39 +158,80 @@ __global__ void __launch_bounds__(kCtThreads, 2)
     };
 
     if (warp >= 4 && warp < 8) {
-        // ---- producers: A1 = YB_l rows, B1 = W_l rows of the a tile, per K stage of 32 atoms b
+        // ---- producers: A1 = YB_l rows, B1 = W_l rows of the a tile, per K
+        // stage of 32 atoms b.  The next stage's values are loaded into
+        // registers before the wait for its buffer, so the global loads of
+        // one stage overlap the hand-over of the previous one.
         const int r = tid - 128;
         int j = 0;
-        bool ok = true;
-        for (int gi = 0; gi < P.ngroups && ok; ++gi) {
-            const GroupDev g = groups[P.group0 + gi];
-            const int n = g.n, nk = (n + kCtK - 1) / kCtK;
+        float2 ya[kCtAUnits][4];
+        float wb[2][4];
+        // stage (group gi, tile a0, chunk kc) -> registers
+        auto load = [&](const GroupDev &g, int a0, int kc) {
+            const int n = g.n, k0 = kc * kCtK;
             const float2 *yb = ytB + yoff + (g.slot0 - P.atom0);
             const float *w = wt + g.w0 + (long long)l * n * n;
-            for (int a0 = 0; a0 < n && ok; a0 += kCtTile)
-                for (int kc = 0; kc < nk; ++kc, ++j) {
-                    const int s = j & 1;
-                    if (j >= 2 && !mbar_wait(empty(s), ((j >> 1) - 1) & 1, abort)) { give_up(); ok = false; break; }
-                    const int k0 = kc * kCtK;
-                    unsigned char *ah = gen(a1_addr(s, 0)), *al = gen(a1_addr(s, 1));
-                    for (int u = r; u < ni * 8; u += 128) {
-                        const int i = u >> 3, q = u & 7;
-                        stage_y(yb + (long long)i * P.n, k0 + 4 * q, n, i, q, ah, al);
-                    }
-                    unsigned char *bh = gen(b1_addr(s, 0)), *bl = gen(b1_addr(s, 1));
-                    for (int u = r; u < kCtTile * 8; u += 128) {
-                        const int ar = u >> 3, q = u & 7, a = a0 + ar, b = k0 + 4 * q;
-                        float v[4];
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) v[e] = (a < n && b + e < n) ? w[(long long)a * n + b + e] : 0.f;
-                        float4 h, lo;
-                        split4(v, h, lo);
-                        *reinterpret_cast<float4 *>(bh + sw128_off(ar, q)) = h;
-                        *reinterpret_cast<float4 *>(bl + sw128_off(ar, q)) = lo;
-                    }
-                    fence_async_smem();   // generic-proxy stores -> visible to the tensor cores
-                    mbar_arrive(full(s));
+            for (int x = 0; x < kCtAUnits; ++x) {
+                const int u = r + 128 * x, i = u >> 3, b = k0 + 4 * (u & 7);
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    ya[x][e] = (u < ni * 8 && b + e < n) ? yb[(long long)i * P.n + b + e] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                const int u = r + 128 * x, a = a0 + (u >> 3), b = k0 + 4 * (u & 7);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) wb[x][e] = (a < n && b + e < n) ? w[(long long)a * n + b + e] : 0.f;
+            }
+        };
+        // the stage sequence: groups, a tiles, K chunks
+        int gi = 0, a0 = 0, kc = 0;
+        GroupDev g = groups[P.group0];
+        load(g, a0, kc);
+        for (;;) {
+            const int s = j & 1;
+            if (j >= 2 && !mbar_wait(empty(s), ((j >> 1) - 1) & 1, abort)) { give_up(); break; }
+            unsigned char *ah = gen(a1_addr(s, 0)), *al = gen(a1_addr(s, 1));
+#pragma unroll
+            for (int x = 0; x < kCtAUnits; ++x) {
+                const int u = r + 128 * x, i = u >> 3, q = u & 7;
+                if (u < ni * 8) {
+                    float re[4], im[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) { re[e] = ya[x][e].x; im[e] = ya[x][e].y; }
+                    float4 h, lo;
+                    split4(re, h, lo);
+                    *reinterpret_cast<float4 *>(ah + sw128_off(2 * i, q)) = h;
+                    *reinterpret_cast<float4 *>(al + sw128_off(2 * i, q)) = lo;
+                    split4(im, h, lo);
+                    *reinterpret_cast<float4 *>(ah + sw128_off(2 * i + 1, q)) = h;
+                    *reinterpret_cast<float4 *>(al + sw128_off(2 * i + 1, q)) = lo;
                 }
+            }
+            unsigned char *bh = gen(b1_addr(s, 0)), *bl = gen(b1_addr(s, 1));
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                const int u = r + 128 * x;
+                float4 h, lo;
+                split4(wb[x], h, lo);
+                *reinterpret_cast<float4 *>(bh + sw128_off(u >> 3, u & 7)) = h;
+                *reinterpret_cast<float4 *>(bl + sw128_off(u >> 3, u & 7)) = lo;
+            }
+            fence_async_smem();   // generic-proxy stores -> visible to the tensor cores
+            mbar_arrive(full(s));
+            ++j;
+            // advance to the next stage and prefetch it
+            if (++kc == (g.n + kCtK - 1) / kCtK) {
+                kc = 0;
+                a0 += kCtTile;
+                if (a0 >= g.n) {
+                    a0 = 0;
+                    if (++gi == P.ngroups) break;
+                    g = groups[P.group0 + gi];
+                }
+            }
+            load(g, a0, kc);
         }
     } else if (warp == 8) {
         // ---- MMA issuer (one thread).  Each accumulator in tensor memory takes

@@ -353,6 +353,10 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
             }
         }
         __syncwarp();
+        // Neighbour-list entries of the row to be scanned next, loaded one
+        // scan ahead: the row of the last column on the label list, which is
+        // the next one taken unless the current scan adds columns to it.
+        int pf_row = -1, pf_col[2] = {-1, -1};
         while (jend < 0) {
             if (++guard > gmax) return 9;
             if (k == 0) return 4;
@@ -362,6 +366,14 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
             __syncwarp();
             if (lane == 0) todo[td] = jc;
             --td;
+            int rcol[2] = {pf_col[0], pf_col[1]};
+            if (!dense && pf_row != i)
+                for (int q = 0; q < 2; ++q) rcol[q] = (lane + 32 * q < m) ? COL(i, lane + 32 * q) : -1;
+            pf_row = -1;
+            if (!dense && k > 0) {
+                pf_row = y[todo[k - 1]];
+                for (int q = 0; q < 2; ++q) pf_col[q] = (lane + 32 * q < m) ? COL(pf_row, lane + 32 * q) : -1;
+            }
             // scan position of jc in row i: jc is the column row i holds, and
             // rows only ever hold columns of their own list
             int tpos = jc;
@@ -383,7 +395,7 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
                 eq[q] = false;
                 jq[q] = -1;
                 if (t < m) {
-                    int j = COL(i, t);
+                    int j = dense ? t : rcol[q];
                     jq[q] = j;
                     if (!ok[j]) {
                         long long vj = cost(i, t, j) - hh - v[j];
@@ -415,18 +427,37 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
             __syncwarp();
             if (jend >= 0) break;
             if (k != 0) continue;
+            // next level: the smallest label among the unscanned columns.  One
+            // pass keeps each lane's minimum, its first column and its count;
+            // a single column at the minimum (the usual case) is taken
+            // directly, ties are collected in index order by a second pass.
             long long lm = kLLMax;
-            for (int j = lane; j < n; j += 32)
-                if (!ok[j] && dd[j] <= kBigInt - 1 && dd[j] < lm) lm = dd[j];
-            lm = wmin_ll(lm);
-            if (lm == kLLMax) { mn = kBigInt - 1; k = 0; continue; }
-            mn = lm;
-            for (int b = 0; b < n; b += 32) {
-                int j = b + lane;
-                bool sel = (j < n) && !ok[j] && dd[j] == mn;
-                unsigned sm = __ballot_sync(kFull, sel);
-                if (sel) todo[k + __popc(sm & ltmask)] = j;
-                k += __popc(sm);
+            int lj = -1, lc = 0;
+#pragma unroll 4
+            for (int j = lane; j < n; j += 32) {
+                const long long dj = dd[j];
+                if (!ok[j] && dj <= kBigInt - 1) {
+                    if (dj < lm) { lm = dj; lj = j; lc = 1; }
+                    else if (dj == lm) ++lc;
+                }
+            }
+            const long long wm = wmin_ll(lm);
+            if (wm == kLLMax) { mn = kBigInt - 1; k = 0; continue; }
+            mn = wm;
+            const int nat = __reduce_add_sync(kFull, lm == wm ? lc : 0);
+            if (nat == 1) {
+                const unsigned who = __ballot_sync(kFull, lm == wm);
+                const int j1 = __shfl_sync(kFull, lj, __ffs(who) - 1);
+                if (lane == 0) todo[0] = j1;
+                k = 1;
+            } else {
+                for (int b = 0; b < n; b += 32) {
+                    int j = b + lane;
+                    bool sel = (j < n) && !ok[j] && dd[j] == mn;
+                    unsigned sm = __ballot_sync(kFull, sel);
+                    if (sel) todo[k + __popc(sm & ltmask)] = j;
+                    k += __popc(sm);
+                }
             }
             __syncwarp();
             for (int b = 0; b < k && jend < 0; b += 32) {
