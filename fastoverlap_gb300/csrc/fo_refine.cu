@@ -1130,12 +1130,10 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
     if constexpr (RECOMP) {
         auto run = [&](const auto &cf) {
             if (!dense) {
-                if (ns <= kHeapMaxRow) {   // a heap per lane, one row each (32 rows at once)
-                    float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
-                    for (int i = lane; i < ns; i += 32)
-                        nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
-                } else if (cmd && thr && ns <= 32 * kNearRegMW) {
-                    // every warp of the block on its own rows (the first warp is the caller)
+                if (cmd && thr && ns <= 32 * kNearRegMW) {
+                    // every warp of the block on its own rows (the first warp is
+                    // the caller); in multi-warp blocks this serves the smaller
+                    // sparse groups of the pair as well
                     if (lane == 0) {
                         cmd->op = 1;
                         cmd->ns = ns;
@@ -1151,6 +1149,10 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                     named_bar(1, blockDim.x);
                     nbr_rows<KT, BOX>(*cmd, 0, blockDim.x >> 5);
                     named_bar(2, blockDim.x);
+                } else if (ns <= kHeapMaxRow) {   // a heap per lane, one row each (32 rows at once)
+                    float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
+                    for (int i = lane; i < ns; i += 32)
+                        nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
                 } else {   // the warp on one row at a time, from the row's last m-th distance when warm
                     float *dr = (float *)(lb + L.lap_heap);
                     for (int i = 0; i < ns; ++i)
