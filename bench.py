@@ -44,6 +44,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 METRIC = "aligned pairs/s (batched+mixed vs plain FP64 GPU, RMSD-matched); p50/p99 ms"
+# Warp instructions the refinement kernel issues per candidate on the 4096-pair
+# workload (mixed form): smsp__inst_executed.sum over the seven bucket launches
+# of one plan run (ncu), divided by the plan's candidates.
+REFINE_INST_PER_CAND = 180246.0   # 14.70e9 over 81,574 candidates
 WORKLOAD = ("c2: 4096 batched spherical pairs, N~U{13..147}, 1-3 species, Jmax~{7,11,15}, "
             "sigma 0.3, 10 peaks/orientation, inversion")
 
@@ -527,6 +531,28 @@ def main():
             "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_src,
             "kernel_ms_per_launch": top_ms,
             "kernel_share": kern[top][0] / sum(v[0] for v in kern.values())}
+    cfg_extra["candidates_per_step"] = int(np.sum(r["ncand"]))
+    if top == "refine" and REFINE_INST_PER_CAND:
+        # The refinement is bound by issue latency along each warp's sequential
+        # assignment steps (ncu: 0.2 eligible warps per scheduler cycle, `wait`
+        # stalls first, 0.6 KB of DRAM traffic per candidate), so its roofline
+        # is the issue-slot one: warp instructions issued per second against
+        # one per scheduler per cycle.  Instructions of one run of this
+        # workload's plan, from an ncu capture of its seven bucket launches
+        # (smsp__inst_executed.sum), scaled by the step's candidates; the
+        # HBM model above is kept as hbm_model.
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        mhz = float(pk.get("sm_max_mhz", 2070.0)) if peak_src == "measured" else 2070.0
+        peak_i = sms * 4 * mhz * 1e6
+        inst = REFINE_INST_PER_CAND * float(np.sum(r["ncand"]))
+        ach_i = inst / (top_ms / 1000.0)
+        hbm_model = {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac")}
+        roof.update({"bound": "issue", "achieved": ach_i / 1e9, "peak": peak_i / 1e9,
+                     "unit": "G warp-instructions/s", "frac": ach_i / peak_i,
+                     "peak_source": "%d SMs x 4 schedulers x %.0f MHz (one warp instruction per scheduler "
+                                    "per cycle)" % (sms, mhz),
+                     "hbm_model": hbm_model})
     launches = batch.plan_launches() * args.steps
     chunk, group = batch.plan_tile_shape()
     if chunk:
