@@ -556,7 +556,7 @@ def main():
     launches = batch.plan_launches() * args.steps
     chunk, group = batch.plan_tile_shape()
     if chunk:
-        cfg_extra["tc_tile_shape"] = {"wigner_pairs_per_chunk": chunk, "fft_pairs_per_block": group,
+        cfg_extra["tc_tile_shape"] = {"wigner_mm_per_cta": chunk, "fft_pairs_per_block": group,
                                       "picked_by": "autotuner (timed per plan shape, cached per context)"}
 
     if args.c3_pairs > 0:
