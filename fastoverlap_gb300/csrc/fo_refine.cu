@@ -963,6 +963,73 @@ __device__ __forceinline__ void nearest_heap(DT *hd, KT *hk, int ns, int m, cons
     }
 }
 
+// The m nearest columns of each lane's own row (mixed form, rows of at most
+// kHeapMaxRow columns, 32 rows at once): the m smallest squared distances
+// dist(j), j < ns (m < ns), as column indices in increasing order, ties at
+// the m-th value to the lowest indices; the same set as the PAIRDISTS heap
+// whenever the m-th and (m+1)-th distances differ.  Each lane bisects on the
+// bit patterns of its row's distances (recomputed per pass; all lanes read
+// the same column at a time) until a threshold has exactly m distances below
+// it, starting from the bracket [0.99 thr, 1.01 thr] of its previous m-th
+// distance when warm, and stores the new one.  Replaces a heap per lane,
+// whose sift steps cost several times more.
+template <typename KT, typename DF>
+__device__ void nearest_lane(KT *krow, const int ns, const int m, const DF &dist, float *thr, bool warm) {
+    auto count_below = [&](unsigned t) -> int {
+        int c = 0;
+#pragma unroll 4
+        for (int j = 0; j < ns; ++j) c += __float_as_uint(dist(j)) < t;
+        return c;
+    };
+    unsigned lo = 0, hi = 0x7f800000u, v = 0;
+    bool exact = false;
+    const float g = warm ? *thr : 0.f;
+    if (g <= 0.f) {   // cold: bisect between the row's smallest and largest distance
+        unsigned mn = 0x7f800000u, mx = 0;
+#pragma unroll 4
+        for (int j = 0; j < ns; ++j) {
+            const unsigned u = __float_as_uint(dist(j));
+            mn = min(mn, u);
+            mx = max(mx, u);
+        }
+        lo = mn;                            // count(< mn) = 0 <= m
+        hi = mx < 0x7f800000u ? mx + 1 : mx;   // count(< mx + 1) = ns > m
+    } else {
+        const unsigned a = __float_as_uint(g * 0.99f), b = __float_as_uint(g * 1.01f);
+        const int ca = count_below(a);
+        if (ca == m) { exact = true; v = a; }
+        else if (ca > m) hi = a;
+        else {
+            lo = a;
+            const int cb = count_below(b);
+            if (cb == m) { exact = true; v = b; }
+            else if (cb > m) hi = b;
+            else lo = b;
+        }
+    }
+    while (!exact && hi - lo > 1u) {
+        const unsigned mid = lo + (hi - lo) / 2u;
+        const int c = count_below(mid);
+        if (c == m) { exact = true; v = mid; }
+        else if (c < m) lo = mid;
+        else hi = mid;
+    }
+    int need_eq = 0;
+    if (!exact) {   // lo is the m-th smallest: ties at lo, lowest index first
+        v = lo;
+        need_eq = m - count_below(v);
+    }
+    *thr = __uint_as_float(v);
+    int out = 0;
+    for (int j = 0; j < ns && out < m; ++j) {
+        const unsigned u = __float_as_uint(dist(j));
+        if (u < v || (u == v && need_eq > 0)) {
+            if (u == v) --need_eq;
+            krow[out++] = (KT)j;
+        }
+    }
+}
+
 // The m nearest columns of one row (mixed form): the m smallest squared
 // distances dist(j), j < ns (m < ns), as column indices in increasing order;
 // ties at the m-th value go to the lowest indices.  The whole warp works on
@@ -1149,6 +1216,9 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                     named_bar(1, blockDim.x);
                     nbr_rows<KT, BOX>(*cmd, 0, blockDim.x >> 5);
                     named_bar(2, blockDim.x);
+                } else if (ns <= kHeapMaxRow && thr) {   // one row per lane (32 rows at once)
+                    for (int i = lane; i < ns; i += 32)
+                        nearest_lane<KT>(kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); }, thr + i, warm);
                 } else if (ns <= kHeapMaxRow) {   // a heap per lane, one row each (32 rows at once)
                     float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
                     for (int i = lane; i < ns; i += 32)
