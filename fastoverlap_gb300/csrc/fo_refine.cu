@@ -390,26 +390,39 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
             const long long hh = cost(i, tpos, jc) - v[jc] - mn;
             bool eq[2];
             int jq[2];
+            // every load of the row's entries is issued at once (nothing of
+            // these columns is written before the compares below), so the
+            // scan waits for one round of shared-memory latency
+            bool okq[2];
+            long long cq[2], vq[2], dq[2];
+            int yq[2];
+#pragma unroll
             for (int q = 0; q < 2; ++q) {
-                int t = lane + 32 * q;
+                const int t = lane + 32 * q;
+                const bool in = t < m;
+                const int j = in ? (dense ? t : rcol[q]) : 0;
+                jq[q] = in ? j : -1;
+                okq[q] = in ? ok[j] != 0 : true;
+                cq[q] = in ? cost(i, t, j) : 0;
+                vq[q] = in ? v[j] : 0;
+                dq[q] = in ? dd[j] : 0;
+                yq[q] = in ? y[j] : 0;
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
                 eq[q] = false;
-                jq[q] = -1;
-                if (t < m) {
-                    int j = dense ? t : rcol[q];
-                    jq[q] = j;
-                    if (!ok[j]) {
-                        long long vj = cost(i, t, j) - hh - v[j];
-                        if (vj < dd[j]) {
-                            dd[j] = vj;
-                            lab[j] = i;
-                            eq[q] = (vj == mn);
-                        }
+                if (!okq[q]) {
+                    const long long vj = cq[q] - hh - vq[q];
+                    if (vj < dq[q]) {
+                        dd[jq[q]] = vj;
+                        lab[jq[q]] = i;
+                        eq[q] = (vj == mn);
                     }
                 }
             }
             __syncwarp();
             for (int q = 0; q < 2 && jend < 0; ++q) {
-                bool isf = eq[q] && y[jq[q]] < 0;
+                bool isf = eq[q] && yq[q] < 0;
                 unsigned em = __ballot_sync(kFull, eq[q]), fm = __ballot_sync(kFull, isf);
                 unsigned upto = em;
                 if (fm) {
