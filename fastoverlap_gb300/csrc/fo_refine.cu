@@ -185,14 +185,23 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
             y[j] = bi;
         }
     } else {
-        // rows in order; a row's columns are distinct, so lanes never collide
+        // rows in order; a row's columns are distinct, so lanes never collide.
+        // The next row's neighbour-list entries are loaded one row ahead.
         for (int j = lane; j < n; j += 32) { v[j] = kBigInt; y[j] = -1; }
         __syncwarp();
+        int nx[2];
+        for (int q = 0; q < 2; ++q) nx[q] = (lane + 32 * q < m) ? COL(0, lane + 32 * q) : -1;
         for (int i = 0; i < n; ++i) {
-            for (int t = lane; t < m; t += 32) {
-                const int j = COL(i, t);
-                const long long c = cost(i, t, j);
-                if (c < v[j]) { v[j] = c; y[j] = i; }
+            const int cur[2] = {nx[0], nx[1]};
+            if (i + 1 < n)
+                for (int q = 0; q < 2; ++q) nx[q] = (lane + 32 * q < m) ? COL(i + 1, lane + 32 * q) : -1;
+            for (int q = 0; q < 2; ++q) {
+                const int t = lane + 32 * q;
+                if (t < m) {
+                    const int j = cur[q];
+                    const long long c = cost(i, t, j);
+                    if (c < v[j]) { v[j] = c; y[j] = i; }
+                }
             }
             __syncwarp();
         }
@@ -220,7 +229,12 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
 
     // 2. reduction transfer, rows in order
     int nfree = 0;
+    int nx2[2];
+    for (int q = 0; q < 2; ++q) nx2[q] = (lane + 32 * q < m) ? COL(0, lane + 32 * q) : -1;
     for (int i = 0; i < n; ++i) {
+        const int cur[2] = {nx2[0], nx2[1]};   // this row's entries; the next row's are loaded ahead
+        if (i + 1 < n)
+            for (int q = 0; q < 2; ++q) nx2[q] = (lane + 32 * q < m) ? COL(i + 1, lane + 32 * q) : -1;
         const int xi = x[i];
         if (xi < 0) {
             if (lane == 0) fr[nfree] = i;
@@ -229,8 +243,10 @@ __device__ int jv_warp(const int n, const int m, const bool dense, const CF &cos
         }
         if (ok[i]) continue;
         long long mn = kBigInt;
-        for (int t = lane; t < m; t += 32) {
-            const int j = COL(i, t);
+        for (int q = 0; q < 2; ++q) {
+            const int t = lane + 32 * q;
+            if (t >= m) continue;
+            const int j = cur[q];
             if (j == xi) continue;
             const long long h = cost(i, t, j) - v[j];
             mn = h < mn ? h : mn;
