@@ -1245,13 +1245,9 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
                     named_bar(1, blockDim.x);
                     nbr_rows<KT, BOX>(*cmd, 0, blockDim.x >> 5);
                     named_bar(2, blockDim.x);
-                } else if (ns <= kHeapMaxRow && thr) {   // one row per lane (32 rows at once)
+                } else if (ns <= kHeapMaxRow) {   // one row per lane (32 rows at once)
                     for (int i = lane; i < ns; i += 32)
                         nearest_lane<KT>(kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); }, thr + i, warm);
-                } else if (ns <= kHeapMaxRow) {   // a heap per lane, one row each (32 rows at once)
-                    float *hd = (float *)(lb + L.lap_heap) + lane * kHeapStride;
-                    for (int i = lane; i < ns; i += 32)
-                        nearest_heap<float, KT>(hd, kk + i * m, ns, m, [&](int j) { return cf.d2(i, j); });
                 } else {   // the warp on one row at a time, from the row's last m-th distance when warm
                     float *dr = (float *)(lb + L.lap_heap);
                     for (int i = 0; i < ns; ++i)

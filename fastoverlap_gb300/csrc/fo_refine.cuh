@@ -13,9 +13,10 @@ struct RefLayout {
 };
 
 // Neighbour lists of groups with more than 60 atoms (mixed form): rows of at
-// most kHeapMaxRow columns are selected by a heap per lane (kHeapStride floats
-// of scratch per lane, odd against bank conflicts), longer rows by the whole
-// warp on one row at a time (one row of distances as scratch).
+// most kHeapMaxRow columns are selected a row per lane (nearest_lane), longer
+// rows by the whole warp on one row at a time (one row of distances as
+// scratch) or by all warps of a multi-warp block.  kHeapStride: floats of
+// scratch per lane of the per-lane heap (odd against bank conflicts).
 constexpr int kHeapMaxRow = 256;
 constexpr int kHeapStride = 61;
 
@@ -70,9 +71,10 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     // neighbour lists it is filling)
     L.lap_heap = L.lap_v;
     size_t scratch = 0;
-    if (recomp && sparse) {
-        const size_t heap = 4 * 32 * (size_t)kHeapStride, row = 4 * (size_t)maxg;
-        scratch = ref_a16(heap > row ? heap : row);   // groups up to maxg use either
+    if (recomp && sparse && maxg > kHeapMaxRow) {
+        // one row of distances for the one-warp selector of rows longer than
+        // kHeapMaxRow; shorter rows are selected a row per lane, in registers
+        scratch = ref_a16(4 * (size_t)maxg);
     }
     const size_t heap_end = L.lap_heap + scratch;
     if (heap_end > p) p = heap_end;
