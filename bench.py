@@ -8,7 +8,7 @@ pass of the whole alignment pipeline over the batch.
   value : batched pairs/s with inputs resident in HBM (resident plan), the
           precision given by --precision (default mixed), device time from
           CUDA events on the library's stream, L2 flushed between steps.
-  e2e   : the same batch through fo_cluster_align_batch with host buffers
+  e2e   : the same batch through fo_cluster_align_batch with page-locked host buffers
           (upload, pipeline, download), wall time.
   config: also reports the plain FP64 GPU form (batched and one pair per
           call), the error of the mixed form against FP64, the large-bandwidth
@@ -433,9 +433,10 @@ def main():
     tot_ms = allmax(dist, sum(step_ms))
     value = args.npairs * ws * args.steps / (tot_ms / 1000.0)
 
-    # end to end through the public batch API with host buffers
+    # end to end through the public batch API with host buffers: inputs and
+    # outputs in page-locked host memory (the caller's arrays registered once)
     e2e_times = []
-    eb = ClusterBatch(ctx, pos1, pos2, perms, Jmax=jm, scale=0.3, nrot=10, invert=True)
+    eb = ClusterBatch(ctx, pos1, pos2, perms, Jmax=jm, scale=0.3, nrot=10, invert=True).pin()
     for s in range(max(2, min(args.steps, 3))):
         barrier(dist)
         t0 = time.time()

@@ -98,6 +98,8 @@ EXPORTS = {
     "fo_set_precision": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fo_set_tensor_cores": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fo_set_autotune": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fo_host_register": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t]),
+    "fo_host_unregister": (ctypes.c_int, [_vp, _vp]),
     "fo_plan_tile_shape": (ctypes.c_int, [_vp, _ip, _ip]),
     "fo_cluster_align_batch": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _dp, _dp, _ip, _ip,
                                               ctypes.c_int, _dp, _ip, _vp]),

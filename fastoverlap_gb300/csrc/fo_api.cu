@@ -464,6 +464,18 @@ fo_status fo_set_autotune(fo_ctx *ctx, int on) {
     return FO_OK;
 }
 
+fo_status fo_host_register(fo_ctx *ctx, void *ptr, size_t bytes) {
+    if (!ctx || !ptr || !bytes) return set_err(ctx, FO_ERR_BAD_ARGS, "null buffer or zero size");
+    cudaSetDevice(ctx->opts.device);
+    return cuda_check(ctx, cudaHostRegister(ptr, bytes, cudaHostRegisterDefault), "cudaHostRegister");
+}
+
+fo_status fo_host_unregister(fo_ctx *ctx, void *ptr) {
+    if (!ctx || !ptr) return set_err(ctx, FO_ERR_BAD_ARGS, "null buffer");
+    cudaSetDevice(ctx->opts.device);
+    return cuda_check(ctx, cudaHostUnregister(ptr), "cudaHostUnregister");
+}
+
 fo_status fo_plan_tile_shape(const fo_plan *pl, int *chunk, int *group) {
     if (!pl || !chunk || !group) return FO_ERR_BAD_ARGS;
     *chunk = pl->tc ? pl->tc_chunk : 0;

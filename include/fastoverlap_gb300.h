@@ -123,10 +123,12 @@ void        fo_ctx_destroy(fo_ctx *ctx);
 const char *fo_status_string(fo_status s);
 const char *fo_last_error(const fo_ctx *ctx);
 fo_status   fo_set_precision(fo_ctx *ctx, int precision);
-/* Mixed form: 1 (default) runs the Wigner-d contraction of the inverse SO(3)
- * transform (ISOFT, fastoverlap/f90/DSOFT.f90:286-299) on the tcgen05 tensor
- * cores in split TF32 (3xTF32, FP32 accumulation); 0 on the FP32 CUDA cores.
- * Applies to plans created afterwards; the FP64 form never uses it.          */
+/* Mixed form: 1 (default) runs the coefficient contraction (FOURIERCOEFFS,
+ * fastoverlap/f90/fastclusters.f90:905-911) and the Wigner-d contraction of
+ * the inverse SO(3) transform (ISOFT, fastoverlap/f90/DSOFT.f90:286-299) on
+ * the tcgen05 tensor cores in split TF32 (3xTF32, FP32 accumulation); 0 on
+ * the FP32 CUDA cores.  Applies to plans created afterwards; the FP64 form
+ * never uses it.                                                             */
 fo_status   fo_set_tensor_cores(fo_ctx *ctx, int on);
 /* No counterpart in the reference.  1 (default): a mixed-form plan of at
  * least 256 pairs whose shape (distinct Jmax values, pair count rounded up
@@ -137,6 +139,12 @@ fo_status   fo_set_tensor_cores(fo_ctx *ctx, int on);
  * 0: the default shape (64, 1).  fo_plan_tile_shape reports a plan's shape
  * (0, 0 when it does not use the tensor cores).                             */
 fo_status   fo_set_autotune(fo_ctx *ctx, int on);
+/* No counterpart in the reference.  Page-lock a caller's host buffer of
+ * `bytes` bytes (cudaHostRegister) so that the batched entry points copy it
+ * to and from the device by DMA; fo_host_unregister releases it.  The buffer
+ * stays the caller's memory throughout.                                      */
+fo_status   fo_host_register(fo_ctx *ctx, void *ptr, size_t bytes);
+fo_status   fo_host_unregister(fo_ctx *ctx, void *ptr);
 
 /* ---- batched entry points (host buffers in, host buffers out) ----
  * pos1 = target structures (COORDSB), pos2 = structures moved onto them
