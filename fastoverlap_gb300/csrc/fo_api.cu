@@ -6,6 +6,7 @@
 #include "fo_kernels.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
@@ -14,6 +15,7 @@
 #include <numeric>
 #include <tuple>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fo_refine.cuh"
@@ -187,6 +189,36 @@ fo_status ensure_tc_tables(fo_ctx *ctx, const std::vector<int> &bws) {
     return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "tensor-core Wigner tables");
 }
 
+// f(i) for i < n on host threads, in chunks of 16 (serially for small n)
+template <typename F>
+void host_parallel(int n, const F &f) {
+    const int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 16u);
+    if (n < 256 || nt <= 1) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int> next(0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&] {
+            for (int i0; (i0 = next.fetch_add(16)) < n;)
+                for (int i = i0; i < std::min(n, i0 + 16); ++i) f(i);
+        });
+    for (auto &x : th) x.join();
+}
+
+double centred_radius(const double *X, int n);
+
+// The O(natoms) host work of plan creation for every pair, on host threads:
+// the permutation groups (slot2orig at the pair's atom offset), finite
+// coordinates, and (dmax != nullptr) the sum of both structures' centred
+// radii.  bad[i] = 1 marks a pair that fails either check; the caller reports
+// the first failing pair in pair order with check_groups' or its own message.
+template <typename PairT>
+void host_pair_checks(int npairs, const PairT *pairs, const double *pos1, const double *pos2, const int *perm,
+                      const int *gsizes, int base, std::vector<long long> &aoff, std::vector<int> &s2o,
+                      std::vector<char> &bad, std::vector<double> *dmax);
+
 // validate the permutation groups of one pair and fill slot2orig
 fo_status check_groups(fo_ctx *ctx, int i, int n, int ngroups, const int *perm,
                        const int *gsizes, int base, int *slot2orig) {
@@ -207,6 +239,41 @@ fo_status check_groups(fo_ctx *ctx, int i, int n, int ngroups, const int *perm,
         slot2orig[s] = a;
     }
     return FO_OK;
+}
+
+template <typename PairT>
+void host_pair_checks(int npairs, const PairT *pairs, const double *pos1, const double *pos2, const int *perm,
+                      const int *gsizes, int base, std::vector<long long> &aoff, std::vector<int> &s2o,
+                      std::vector<char> &bad, std::vector<double> *dmax) {
+    aoff.assign(npairs + 1, 0);
+    for (int i = 0; i < npairs; ++i) aoff[i + 1] = aoff[i] + std::max(0, std::min(pairs[i].natoms, kMaxAtoms));
+    s2o.assign((size_t)aoff[npairs], 0);
+    bad.assign(npairs, 0);
+    if (dmax) dmax->assign(npairs, 0.0);
+    host_parallel(npairs, [&](int i) {
+        const PairT &q = pairs[i];
+        const int n = q.natoms;
+        if (n < 1 || n > kMaxAtoms) return;   // reported by the scalar checks
+        int *so = s2o.data() + aoff[i];
+        const int *pm = perm + q.perm_off, *gs = gsizes + q.group_off;
+        long long tot = 0;
+        for (int g = 0; g < q.ngroups; ++g) {
+            if (gs[g] < 0) { bad[i] = 1; return; }
+            tot += gs[g];
+        }
+        if (q.ngroups < 1 || tot != n) { bad[i] = 1; return; }
+        std::vector<char> seen(n, 0);
+        for (int t = 0; t < n; ++t) {
+            const int a = pm[t] - base;
+            if (a < 0 || a >= n || seen[a]) { bad[i] = 1; return; }
+            seen[a] = 1;
+            so[t] = a;
+        }
+        const double *x1 = pos1 + 3 * q.coord_off, *x2 = pos2 + 3 * q.coord_off;
+        for (int k = 0; k < 3 * n; ++k)
+            if (!std::isfinite(x1[k]) || !std::isfinite(x2[k])) { bad[i] = 1; return; }
+        if (dmax) (*dmax)[i] = centred_radius(x1, n) + centred_radius(x2, n);
+    });
 }
 
 struct Carve {
@@ -875,6 +942,11 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
     long long ylm_n = 0, w_n = 0, coef_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
     int atom0 = 0, cand0 = 0;
     const bool contig = packed_in_order(pairs, npairs);   // upload straight from the caller's arrays
+    std::vector<long long> aoff;
+    std::vector<int> s2o_all;
+    std::vector<char> bad;
+    std::vector<double> dmaxv;
+    host_pair_checks(npairs, pairs, pos1, pos2, perm, group_sizes, index_base, aoff, s2o_all, bad, &dmaxv);
     for (int i = 0; i < npairs; ++i) {
         const fo_cluster_pair &q = pairs[i];
         const int n = q.natoms, L = q.jmax;
@@ -883,13 +955,13 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
         if (q.nrot < 1 || q.nrot > kMaxNrot) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: nrot %d outside [1,%d]", i, q.nrot, kMaxNrot); }
         if (!(q.sigma == q.sigma)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: sigma is NaN", i); }
         if (harm_n >= 0 && !(q.sigma > 0.0)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: the harmonic basis needs sigma > 0", i); }
-        std::vector<int> s2o(n);
-        fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
-                                   index_base, s2o.data());
-        if (s) { delete pl; return s; }
-        for (int k = 0; k < 3 * n; ++k) {
-            double a = pos1[3 * q.coord_off + k], b = pos2[3 * q.coord_off + k];
-            if (!std::isfinite(a) || !std::isfinite(b)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: non-finite coordinate", i); }
+        const int *s2o = s2o_all.data() + aoff[i];
+        if (bad[i]) {   // the same checks again, serially, for the message
+            std::vector<int> tmp(n);
+            fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
+                                       index_base, tmp.data());
+            delete pl;
+            return s ? s : set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: non-finite coordinate", i);
         }
         fo::PairDev P{};
         P.n = n;
@@ -926,8 +998,7 @@ static fo_status cluster_plan_create(fo_ctx *ctx, int npairs, const fo_cluster_p
             pl->hg.push_back(G);
         }
         {
-            double dmax = centred_radius(pos1 + 3 * q.coord_off, n) + centred_radius(pos2 + 3 * q.coord_off, n);
-            RefAssign ra = ref_assign(n, maxg, pl->fp32, pl->fp32, dmax);
+            RefAssign ra = ref_assign(n, maxg, pl->fp32, pl->fp32, dmaxv[i]);
             P.lapstride = ra.lapstride;
             P.lapsplit = ra.split;
             P.lap0 = lap_total;
@@ -1021,6 +1092,10 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
     long long fgrid_n = 0, grid_n = 0, lap_total = 0, candatom = 0;
     int atom0 = 0, cand0 = 0;
     const bool contig = packed_in_order(pairs, npairs);   // upload straight from the caller's arrays
+    std::vector<long long> aoff;
+    std::vector<int> s2o_all;
+    std::vector<char> bad;
+    host_pair_checks(npairs, pairs, pos1, pos2, perm, group_sizes, index_base, aoff, s2o_all, bad, nullptr);
     for (int i = 0; i < npairs; ++i) {
         const fo_bulk_pair &q = pairs[i];
         const int n = q.natoms;
@@ -1034,13 +1109,13 @@ fo_status fo_bulk_plan_create(fo_ctx *ctx, int npairs, const fo_bulk_pair *pairs
         if (M < 2 * K + 1 || M > kMaxM) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: nfspace %d must lie in [2K+1, %d]", i, M, kMaxM); }
         if (nd > kMaxNrot) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: ndisps %d > %d", i, nd, kMaxNrot); }
         if (q.ohcell) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: ohcell pairs run through fo_bulk_align_batch, not plans", i); }
-        std::vector<int> s2o(n);
-        fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
-                                   index_base, s2o.data());
-        if (s) { delete pl; return s; }
-        for (int k = 0; k < 3 * n; ++k) {
-            double a = pos1[3 * q.coord_off + k], b = pos2[3 * q.coord_off + k];
-            if (!std::isfinite(a) || !std::isfinite(b)) { delete pl; return set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: non-finite coordinate", i); }
+        const int *s2o = s2o_all.data() + aoff[i];
+        if (bad[i]) {   // the same checks again, serially, for the message
+            std::vector<int> tmp(n);
+            fo_status s = check_groups(ctx, i, n, q.ngroups, perm + q.perm_off, group_sizes + q.group_off,
+                                       index_base, tmp.data());
+            delete pl;
+            return s ? s : set_err(ctx, FO_ERR_BAD_ARGS, "pair %d: non-finite coordinate", i);
         }
         fo::PairDev P{};
         P.n = n;
