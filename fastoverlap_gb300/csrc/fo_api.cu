@@ -198,12 +198,16 @@ void host_parallel(int n, const F &f) {
         return;
     }
     std::atomic<int> next(0);
+    auto work = [&] {
+        for (int i0; (i0 = next.fetch_add(16)) < n;)
+            for (int i = i0; i < std::min(n, i0 + 16); ++i) f(i);
+    };
     std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t)
-        th.emplace_back([&] {
-            for (int i0; (i0 = next.fetch_add(16)) < n;)
-                for (int i = i0; i < std::min(n, i0 + 16); ++i) f(i);
-        });
+    try {
+        for (int t = 1; t < nt; ++t) th.emplace_back(work);
+    } catch (...) {   // no more threads: the ones started and this one finish the work
+    }
+    work();
     for (auto &x : th) x.join();
 }
 

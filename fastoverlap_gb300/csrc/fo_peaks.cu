@@ -311,7 +311,13 @@ __device__ __forceinline__ void warp_argmax_finish(T best, int bi, double s, T &
 // them, so the depth of its load pipeline sets their speed on large grids
 // (edge >= kDeepGrid: 16 loads per lane, measured 20.8 -> 12.8 ms for 64^3
 // grids); grids of edge <= 32 measured faster with 4.
-constexpr int kDeepGrid = 48;
+#ifndef FO_DEEP_GRID
+#define FO_DEEP_GRID 48
+#endif
+#ifndef FO_DEEP_UNROLL
+#define FO_DEEP_UNROLL 16
+#endif
+constexpr int kDeepGrid = FO_DEEP_GRID;
 
 // (max value, first index) and sum over a grid of N points by one warp;
 // U loads in flight per lane.
@@ -406,7 +412,7 @@ __global__ void __launch_bounds__(32, FO_PEAKS_MINB) k_findpeaks(const PairDev *
     int amax;
     double sum;
     const bool deep = G >= kDeepGrid;
-    if (deep) warp_argmax_sum<T, 16>(f, N, mx, amax, sum);
+    if (deep) warp_argmax_sum<T, FO_DEEP_UNROLL>(f, N, mx, amax, sum);
     else warp_argmax_sum<T>(f, N, mx, amax, sum);
     if (lane == 0) omax[2 * p + o] = (double)mx;
     int nfound = 0;
@@ -446,7 +452,7 @@ __global__ void __launch_bounds__(32, FO_PEAKS_MINB) k_findpeaks(const PairDev *
         ++nfound;
         // subtract the fitted peak (not wrapped) and its mean level; the same
         // pass finds the next first maximum and the new grid sum
-        if (deep) warp_subtract_argmax_sum<T, 16>(f, G, q, c1, c2, c3, mx, amax, sum);
+        if (deep) warp_subtract_argmax_sum<T, FO_DEEP_UNROLL>(f, G, q, c1, c2, c3, mx, amax, sum);
         else warp_subtract_argmax_sum<T>(f, G, q, c1, c2, c3, mx, amax, sum);
     }
     if (lane == 0) npeaks[2 * p + o] = nfound;
