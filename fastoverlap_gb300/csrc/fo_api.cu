@@ -356,12 +356,12 @@ RefAssign ref_assign(int n, int maxg, bool fp32, bool recomp, double dmax) {
     fo::ref_layout(n, maxg, fp32, r.ct64 ? 8 : 4, recomp, L);
     // Footprint classes, one launch each: the largest dynamic shared memory
     // with which k one-warp blocks stay resident on an SM (233472 bytes per
-    // SM, 1 KB reserved per block, the kernel's static arrays), k = 16 (the
-    // register limit of the kernel) down to 1.  A finer class would not fit
-    // more warps on an SM.
+    // SM, 1 KB reserved per block, up to 640 bytes of the kernel's static
+    // arrays: 528 in the multi-warp forms), k = 16 (the register limit of the
+    // kernel) down to 1.  A finer class would not fit more warps on an SM.
     auto up = [](size_t b) {
         for (int k = 16; k >= 1; --k) {
-            const size_t c = ((size_t)233472 / k - 1024 - 512) & ~(size_t)127;
+            const size_t c = ((size_t)233472 / k - 1024 - 640) & ~(size_t)127;
             if (b <= c) return c;
         }
         return (b + 127) & ~(size_t)127;
@@ -590,6 +590,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
            o_cdisp = cv.take<double>(3 * (size_t)nc);
     size_t o_cxyz = cv.take<double>(3 * candatoms), o_cperm = cv.take<int>(candatoms);
     size_t o_cthr = cv.take<float>(pl->fp32 ? candatoms : 0);
+    size_t o_b4 = cv.take<float4>(pl->fp32 ? (size_t)ns : 0), o_cscr = cv.take<int>(pl->fp32 ? 2 * candatoms : 0);
     size_t o_cnit = cv.take<int>(nc), o_cst = cv.take<int>(nc);
     size_t o_res = cv.take<fo_pair_result>(np), o_al = cv.take<double>(3 * (size_t)ns),
            o_pb = cv.take<int>(ns);
@@ -672,6 +673,8 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
     r.cdisp = (double *)P(o_cdisp);
     r.cxyz = (double *)P(o_cxyz);
     r.cthr = (float *)P(o_cthr);
+    r.b4 = (float4 *)P(o_b4);
+    r.cscr = (int *)P(o_cscr);
     r.cperm = (int *)P(o_cperm);
     r.cniter = (int *)P(o_cnit);
     r.cstat = (int *)P(o_cst);
@@ -1359,11 +1362,13 @@ int fo_plan_launches(const fo_plan *pl) {
     if (!pl) return 0;
     int nb = 0;
     for (const auto &b : pl->buckets) nb += b.count > 0;
-    // cluster: centre, ylm, radial, coeff, isoft; bulk: prep, sf, 3 fft passes;
-    // then findpeaks (5^3 window, wider windows), one refinement launch per
-    // bucket, select
-    const int tcl = pl->tc ? (int)pl->tcb.launches.size() + 1 : 0;   // contraction launches and the FFT stage
-    return (pl->bulk ? 5 : 5) + tcl + 2 + nb + 1;
+    // cluster: centre, ylm, radial, coefficients, inverse transform (with the
+    // tensor cores: the FFT stage, after the Wigner contraction's launches);
+    // bulk: prep, sf, 3 fft passes; then findpeaks (5^3 window, wider
+    // windows), the mixed form's fixed-structure copy, one refinement launch
+    // per bucket, select
+    const int tcl = pl->tc ? (int)pl->tcb.launches.size() : 0;
+    return 5 + tcl + 2 + (pl->fp32 ? 1 : 0) + nb + 1;
 }
 
 void fo_plan_destroy(fo_plan *pl) {

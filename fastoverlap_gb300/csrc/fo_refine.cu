@@ -1309,6 +1309,45 @@ __device__ int assign_group(const int ns, const int m, const GroupCoords &G, uns
     }
 }
 
+// Centroids of a pair's two inputs (XA's in mx[0..2], XB's in mx[3..5]),
+// every lane getting all six.  The refinement and k_ref_b4 both use it, so
+// the fixed structure's centred FP32 copy has the same bits in both.
+__device__ __forceinline__ void pair_centroids(const double *XA, const double *XB, int n, int lane,
+                                               double (&mx)[6]) {
+    double v6[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = lane; j < n; j += 32)
+        for (int r = 0; r < 3; ++r) {
+            v6[r] += XA[3 * j + r];
+            v6[3 + r] += XB[3 * j + r];
+        }
+    warp_halve<6>(v6, lane);
+    const double mean = v6[0] / n;
+    for (int r = 0; r < 6; ++r) mx[r] = __shfl_sync(kFull, mean, halve_lane(r, 6));
+}
+
+// Mixed form: the FP32 copy of every pair's fixed structure as the
+// refinement reads it (centred on its centroid for clusters, as given for
+// periodic pairs), one warp per pair, written once to global memory and
+// read by all candidates of the pair (it used to be rebuilt in every
+// candidate's shared memory).
+template <bool BOX>
+__global__ void __launch_bounds__(32) k_ref_b4(const PairDev *pairs, const double *xa, const double *xb,
+                                               float4 *b4) {
+    const int lane = threadIdx.x;
+    const PairDev &P = pairs[blockIdx.x];
+    const int n = P.n, a0 = P.atom0;
+    const double *XA = xa + 3LL * a0, *XB = xb + 3LL * a0;
+    double cm[3] = {0, 0, 0};
+    if constexpr (!BOX) {
+        double mx[6];
+        pair_centroids(XA, XB, n, lane, mx);
+        for (int r = 0; r < 3; ++r) cm[r] = mx[3 + r];
+    }
+    for (int j = lane; j < n; j += 32)
+        b4[a0 + j] = make_float4((float)(XB[3 * j] - cm[0]), (float)(XB[3 * j + 1] - cm[1]),
+                                 (float)(XB[3 * j + 2] - cm[2]), 0.f);
+}
+
 // Resident one-warp blocks per SM the register allocation is sized for
 // (65536 / (32 * FO_REFINE_MINB) registers per thread at most).
 #ifndef FO_REFINE_MINB
@@ -1331,7 +1370,7 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
     k_refine_warp(const PairDev *pairs, const GroupDev *groups, const int *cand_list, const int *cand2pair,
                   const double *xa, const double *xb, const double *peaks, const int *npeaks, unsigned char *lapg,
                   double *cdist, double *cR, double *cdisp, double *cxyz, int *cperm, int *cniter, int *cstat,
-                  float *cthr) {
+                  float *cthr, const float4 *b4g, int *cscr) {
     constexpr bool kF32 = sizeof(DT) == 4;
     static_assert(kF32 || !RECOMP, "costs are recomputed only from FP32 coordinates");
     static_assert(!MW || (kF32 && RECOMP), "helper warps serve the mixed form's neighbour lists only");
@@ -1351,8 +1390,17 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
     for (int gi = 0; gi < P.ngroups; ++gi) maxg = max(maxg, groups[P.group0 + gi].n);
     RefLayout L;
     ref_layout(n, maxg, kF32, (int)sizeof(CT), RECOMP, L);
-    float4 *B4 = (float4 *)(smem + L.DBf), *A4 = (float4 *)(smem + L.DAf);   // mixed form only
-    int *permbest = (int *)(smem + L.perm), *newperm = (int *)(smem + L.nperm), *ptmp = (int *)(smem + L.ptmp);
+    // FP32 coordinate copies: the moved structure per candidate in shared
+    // memory; the fixed structure per pair in global memory (mixed form) or
+    // in shared memory (B4w, the FP32 form with stored costs)
+    float4 *A4 = (float4 *)(smem + L.DAf), *B4w = (float4 *)(smem + L.DBf);
+    const float4 *B4 = RECOMP ? b4g + P.atom0 : B4w;
+    // permutations: the best one in the candidate's output slot and two
+    // working arrays in its global scratch (mixed form), or in shared memory
+    const long long ob = P.candatom0 + (long long)local * n;
+    int *permbest = RECOMP ? cperm + ob : (int *)(smem + L.perm);
+    int *newperm = RECOMP ? cscr + 2 * ob : (int *)(smem + L.nperm);
+    int *ptmp = RECOMP ? cscr + 2 * ob + n : (int *)(smem + L.ptmp);
     // assignment block: on chip; or split (working arrays on chip, costs and
     // neighbour lists in the candidate's global scratch); or all in global
     unsigned char *lbk = P.lapstride ? lapg + P.lap0 + (long long)local * P.lapstride : smem + L.coord_end;
@@ -1360,7 +1408,6 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
     int *lx = (int *)(lb + L.lap_x);
     const double box[3] = {P.box[0], P.box[1], P.box[2]};
     const double *pk = peaks + 3LL * (P.cand0 + o * P.nrot + ci);
-    const long long ob = P.candatom0 + (long long)local * n;
     double *DA = cxyz + 3 * ob;                            // moved structure, FP64
     const double *XA = xa + 3LL * a0, *XB = xb + 3LL * a0;   // inputs of the pair
     if constexpr (kF32 && RECOMP) {
@@ -1404,7 +1451,6 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
                     DA[3 * j + r] = a[r];
                 }
                 A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
-                B4[j] = make_float4((float)XB[3 * j], (float)XB[3 * j + 1], (float)XB[3 * j + 2], 0.f);
                 permbest[j] = j;
             }
         } else {
@@ -1426,16 +1472,8 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
                 sRb[lane] = (lane % 4 == 0) ? 1.0 : 0.0;
             }
             // centroids of both inputs
-            double v6[6] = {0, 0, 0, 0, 0, 0};
-            for (int j = lane; j < n; j += 32)
-                for (int r = 0; r < 3; ++r) {
-                    v6[r] += XA[3 * j + r];
-                    v6[3 + r] += XB[3 * j + r];
-                }
-            warp_halve<6>(v6, lane);
-            const double mean = v6[0] / n;
             double mx[6];
-            for (int r = 0; r < 6; ++r) mx[r] = __shfl_sync(kFull, mean, halve_lane(r, 6));
+            pair_centroids(XA, XB, n, lane, mx);
             __syncwarp();
             // centroid of the rotated moved structure, lanes 0-2
             const int r3 = lane % 3;
@@ -1463,7 +1501,6 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
                     s = fma(b[r], b[r], s);
                 }
                 A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
-                B4[j] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.f);
                 permbest[j] = j;
             }
             S = wsum_d(s);
@@ -1621,8 +1658,7 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
                     DA[3 * j + r] = fma(T[3 * r], x0, fma(T[3 * r + 1], x1, fma(T[3 * r + 2], x2, T[9 + r])));
             }
         }
-        __syncwarp();
-        for (int j = lane; j < n; j += 32) cperm[ob + j] = permbest[j];
+        __syncwarp();   // permbest is the candidate's output slot
         for (int o2 = 16; o2 > 0; o2 >>= 1) fail += __shfl_xor_sync(kFull, fail, o2);
         if constexpr (BOX) {
             if (lane < 9) cR[9LL * c + lane] = (lane % 4 == 0) ? 1.0 : 0.0;
@@ -1702,7 +1738,7 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
                 double b[3];
                 GC.b(j, b);
                 A4[j] = make_float4((float)a[0], (float)a[1], (float)a[2], 0.f);
-                B4[j] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.f);
+                B4w[j] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.f);
             }
             permbest[j] = j;
         }
@@ -1981,6 +2017,10 @@ int refine_block_warps(bool bulk, bool ct64, size_t smem) {
 // events on the main stream) so that small and large problems share the SMs.
 void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux, int naux,
                    cudaEvent_t fork, cudaEvent_t *join) {
+    if (b.fp32 && b.recomp) {
+        if (b.bulk) k_ref_b4<true><<<b.npairs, 32, 0, main>>>(b.pairs, b.xa, b.xb, b.b4);
+        else k_ref_b4<false><<<b.npairs, 32, 0, main>>>(b.pairs, b.xa, b.xb, b.b4);
+    }
     cudaEventRecord(fork, main);
     for (int a = 0; a < naux; ++a) cudaStreamWaitEvent(aux[a], fork, 0);
     for (int k = 0; k < b.nbuckets; ++k) {
@@ -1993,14 +2033,14 @@ void launch_refine(const RefineBuffers &b, cudaStream_t main, cudaStream_t *aux,
         allow_max_smem<k_refine_warp<DT, CT, RC, BX>>();                                             \
         k_refine_warp<DT, CT, RC, BX><<<bk.count, 32, bk.smem, s>>>(                                  \
             b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,      \
-            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat, b.cthr);                               \
+            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat, b.cthr, b.b4, b.cscr);                 \
     } while (0)
 #define FO_LAUNCH_REFINE_MW(CT, BX)                                                                   \
     do {                                                                                              \
         allow_max_smem<k_refine_warp<float, CT, true, BX, true>>();                                  \
         k_refine_warp<float, CT, true, BX, true><<<bk.count, 32 * bk.nw, bk.smem, s>>>(               \
             b.pairs, b.groups, list, b.cand2pair, b.xa, b.xb, b.peaks, b.npeaks, b.lap, b.cdist,      \
-            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat, b.cthr);                               \
+            b.cR, b.cdisp, b.cxyz, b.cperm, b.cniter, b.cstat, b.cthr, b.b4, b.cscr);                 \
     } while (0)
         if (b.fp32 && b.recomp && bk.nw > 1) {
             if (b.bulk) {

@@ -45,12 +45,16 @@ __host__ __device__ inline int ref_kkbytes(int maxg) { return maxg <= 256 ? 1 : 
 // refinement keeps them in global memory.
 __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsize, bool recomp,
                                            RefLayout &L) {
+    // recomp (mixed form): the fixed structure's FP32 copy and the
+    // permutations live in global memory, only the moved structure's FP32
+    // copy and the assignment arrays on chip
     size_t o = 0;
-    L.DBf = o; o += fp32 ? 16 * (size_t)n : 0;
+    L.DBf = o; o += (fp32 && !recomp) ? 16 * (size_t)n : 0;
     L.DAf = o; o += fp32 ? 16 * (size_t)n : 0;
-    L.perm = o; o += ref_a16(4 * (size_t)n);
-    L.nperm = o; o += ref_a16(4 * (size_t)n);
-    L.ptmp = o; o += ref_a16(4 * (size_t)n);
+    const size_t pn = recomp ? 0 : ref_a16(4 * (size_t)n);
+    L.perm = o; o += pn;
+    L.nperm = o; o += pn;
+    L.ptmp = o; o += pn;
     L.coord_end = o;
     const int m = maxg < 60 ? maxg : 60;
     const bool sparse = maxg > 60;
