@@ -590,7 +590,7 @@ static fo_status plan_common_alloc(fo_ctx *ctx, fo_plan *pl, const double *pos1,
            o_cdisp = cv.take<double>(3 * (size_t)nc);
     size_t o_cxyz = cv.take<double>(3 * candatoms), o_cperm = cv.take<int>(candatoms);
     size_t o_cthr = cv.take<float>(pl->fp32 ? candatoms : 0);
-    size_t o_b4 = cv.take<float4>(pl->fp32 ? (size_t)ns : 0), o_cscr = cv.take<int>(pl->fp32 ? 2 * candatoms : 0);
+    size_t o_b4 = cv.take<float4>(pl->fp32 ? (size_t)ns : 0), o_cscr = cv.take<int>(pl->fp32 ? 3 * candatoms : 0);
     size_t o_cnit = cv.take<int>(nc), o_cst = cv.take<int>(nc);
     size_t o_res = cv.take<fo_pair_result>(np), o_al = cv.take<double>(3 * (size_t)ns),
            o_pb = cv.take<int>(ns);

@@ -105,7 +105,8 @@ struct RefineBuffers {
     int *cperm, *cniter, *cstat;
     float *cthr;            // per candidate atom: its neighbour-list threshold (mixed form)
     float4 *b4;             // per slot: the fixed structure's FP32 copy (mixed form)
-    int *cscr;              // per candidate atom: two permutation working entries (mixed form)
+    int *cscr;              // per candidate atom: two permutation working entries and the
+                            // assignment's free list (mixed form)
     // final outputs
     void *results;          // fo_pair_result[npairs]
     double *aligned;        // 3 per atom, original order

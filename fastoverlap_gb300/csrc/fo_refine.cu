@@ -1214,14 +1214,15 @@ struct GroupCoords {
 // JOVOSAP for one group).  Returns the assignment's status.
 template <typename KT, typename DT, typename CT, bool RECOMP, bool BOX>
 __device__ int assign_group(const int ns, const int m, const GroupCoords &G, unsigned char *lb, unsigned char *lbk,
-                            const RefLayout &L, float *thr = nullptr, bool warm = false, NbrCmd *cmd = nullptr) {
+                            const RefLayout &L, float *thr = nullptr, bool warm = false, NbrCmd *cmd = nullptr,
+                            int *frg = nullptr) {
     const int lane = threadIdx.x & 31;
     const bool dense = (m == ns);
     constexpr bool kF32 = sizeof(DT) == 4;   // mixed form: no augmenting row reduction
     KT *kk = (KT *)(lbk + L.lap_kk);
     long long *v = (long long *)(lb + L.lap_v), *dd = (long long *)(lb + L.lap_d);
     int *x = (int *)(lb + L.lap_x), *y = (int *)(lb + L.lap_y), *lab = (int *)(lb + L.lap_lab);
-    int *fr = (int *)(lb + L.lap_fr), *todo = (int *)(lb + L.lap_todo);
+    int *fr = frg ? frg : (int *)(lb + L.lap_fr), *todo = (int *)(lb + L.lap_todo);   // frg: free list in global scratch
     unsigned char *ok = lb + L.lap_ok;
     if constexpr (RECOMP) {
         auto run = [&](const auto &cf) {
@@ -1399,8 +1400,9 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
     // working arrays in its global scratch (mixed form), or in shared memory
     const long long ob = P.candatom0 + (long long)local * n;
     int *permbest = RECOMP ? cperm + ob : (int *)(smem + L.perm);
-    int *newperm = RECOMP ? cscr + 2 * ob : (int *)(smem + L.nperm);
-    int *ptmp = RECOMP ? cscr + 2 * ob + n : (int *)(smem + L.ptmp);
+    int *newperm = RECOMP ? cscr + 3 * ob : (int *)(smem + L.nperm);
+    int *ptmp = RECOMP ? cscr + 3 * ob + n : (int *)(smem + L.ptmp);
+    int *frlist = RECOMP ? cscr + 3 * ob + 2 * n : nullptr;   // the assignment's free list (mixed form)
     // assignment block: on chip; or split (working arrays on chip, costs and
     // neighbour lists in the candidate's global scratch); or all in global
     unsigned char *lbk = P.lapstride ? lapg + P.lap0 + (long long)local * P.lapstride : smem + L.coord_end;
@@ -1546,8 +1548,8 @@ __global__ void __launch_bounds__(MW ? 32 * kRefMaxWarps : 32, MW ? FO_REFINE_MI
                 GC.A = DA + 3 * s0;
                 GC.B4 = B4 + s0;
                 GC.A4 = A4 + s0;
-                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0, cmd)
-                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0, cmd);
+                const int rc = (L.kkbytes == 1) ? assign_group<uint8_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0, cmd, frlist)
+                                                : assign_group<uint16_t, DT, CT, RECOMP, BOX>(ns, m, GC, lb, lbk, L, thrc + s0, iter > 0, cmd, frlist);
                 if (rc) fail += 1;
                 __syncwarp();
                 for (int i = lane; i < ns; i += 32) {

@@ -67,7 +67,7 @@ __host__ __device__ inline void ref_layout(int n, int maxg, bool fp32, int ctsiz
     L.lap_x = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_y = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_lab = p; p += ref_a16(4 * (size_t)maxg);
-    L.lap_fr = p; p += ref_a16(4 * (size_t)maxg);
+    L.lap_fr = p; p += recomp ? 0 : ref_a16(4 * (size_t)maxg);   // mixed form: free list in global scratch
     L.lap_todo = p; p += ref_a16(4 * (size_t)maxg);
     L.lap_ok = p; p += ref_a16((size_t)maxg);
     // the neighbour-selection scratch is only used before a group's
