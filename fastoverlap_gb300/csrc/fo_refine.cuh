@@ -15,10 +15,8 @@ struct RefLayout {
 // Neighbour lists of groups with more than 60 atoms (mixed form): rows of at
 // most kHeapMaxRow columns are selected a row per lane (nearest_lane), longer
 // rows by the whole warp on one row at a time (one row of distances as
-// scratch) or by all warps of a multi-warp block.  kHeapStride: floats of
-// scratch per lane of the per-lane heap (odd against bank conflicts).
+// scratch) or by all warps of a multi-warp block.
 constexpr int kHeapMaxRow = 256;
-constexpr int kHeapStride = 61;
 
 // Mixed form, groups of more than kHeapMaxRow atoms: blocks of up to
 // kRefMaxWarps warps per candidate, where the warps beyond the first only
