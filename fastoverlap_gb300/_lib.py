@@ -270,7 +270,8 @@ class Context(object):
         self.check(self.lib.fo_set_autotune(self.h, int(bool(on))))
 
     def set_tensor_cores(self, on):
-        """Mixed form: Wigner contraction on the tcgen05 tensor cores (default) or not."""
+        """Mixed form: the coefficient and Wigner-d contractions on the tcgen05
+        tensor cores (default) or on the FP32 CUDA cores."""
         self.check(self.lib.fo_set_tensor_cores(self.h, int(bool(on))))
 
     def profile(self):
