@@ -45,9 +45,9 @@ sys.path.insert(0, HERE)
 
 METRIC = "aligned pairs/s (batched+mixed vs plain FP64 GPU, RMSD-matched); p50/p99 ms"
 # Warp instructions the refinement kernel issues per candidate on the 4096-pair
-# workload (mixed form): smsp__inst_executed.sum over the seven bucket launches
-# of one plan run (ncu), divided by the plan's candidates.
-REFINE_INST_PER_CAND = 180246.0   # 14.70e9 over 81,574 candidates
+# workload (mixed form): smsp__inst_executed.sum over the bucket launches of
+# one plan run (ncu), divided by the plan's candidates.
+REFINE_INST_PER_CAND = 218932.0   # 17.86e9 over 81,574 candidates
 WORKLOAD = ("c2: 4096 batched spherical pairs, N~U{13..147}, 1-3 species, Jmax~{7,11,15}, "
             "sigma 0.3, 10 peaks/orientation, inversion")
 
@@ -539,7 +539,7 @@ def main():
         # stalls first, 0.6 KB of DRAM traffic per candidate), so its roofline
         # is the issue-slot one: warp instructions issued per second against
         # one per scheduler per cycle.  Instructions of one run of this
-        # workload's plan, from an ncu capture of its seven bucket launches
+        # workload's plan, from an ncu capture of its bucket launches
         # (smsp__inst_executed.sum), scaled by the step's candidates; the
         # HBM model above is kept as hbm_model.
         import torch
