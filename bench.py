@@ -301,19 +301,22 @@ def allmax(dist, v):
 def _oracle_sample(pairs, nthreads, budget_s, per_call=None):
     """The oracle (CPU restatement of the reference algorithm) over a bounded
     sample of the workload, in calls of per_call pairs (default 8 per thread,
-    so that the threads' dynamic pair queue stays balanced), until budget_s
-    of CPU time has passed.  Returns (pairs/s, pairs done, seconds, per_call)."""
+    so that the threads' dynamic pair queue stays balanced): at least one call,
+    then more until budget_s of CPU time has passed.  Returns (pairs/s, pairs
+    done, seconds, per_call)."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import oracle as O
     sample = [dict(pos1=p[0], pos2=p[1], perm=p[2], Jmax=p[3], sigma=0.3) for p in pairs]
     per_call = per_call or 8 * nthreads
     done, dt = 0, 0.0
-    while dt < budget_s:
+    while True:
         chunk = [sample[(done + i) % len(sample)] for i in range(per_call)]
         t0 = time.time()
         O.cluster_align_many(chunk, nrot=10, invert=True, cutoff=True, nthreads=nthreads)
         dt += time.time() - t0
         done += per_call
+        if dt >= budget_s:
+            break
     return done / dt, done, dt, per_call
 
 

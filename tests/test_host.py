@@ -152,6 +152,19 @@ def test_clock_sampler_parses_reasons():
     assert r["sm_mhz"] == 1985 and r["sm_max_mhz"] == 2070 and r["reasons"] == ["sw_power_cap"]
 
 
+def test_reference_arm_sampler_makes_at_least_one_call(oracle_mod):
+    """The CPU sampler behind bench.py --impl reference and the cpu_baseline
+    leg: a zero time budget (one call per reference-arm step) still aligns
+    its pairs and reports a finite rate."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from fastoverlap_gb300 import synth
+    pairs = [(p["pos1"], p["pos2"], [np.asarray(g) for g in p["perm"]], p["Jmax"])
+             for p in synth.config2(2, seed_offset=77)]
+    rate, done, dt, per_call = bench._oracle_sample(pairs, 1, 0.0, 2)
+    assert done == 2 and per_call == 2 and dt > 0 and np.isfinite(rate) and rate > 0
+
+
 def test_batch_result_unpacking_spans():
     """Per-pair views of the packed outputs (no GPU: the unpacking is host code)."""
     import numpy as np
